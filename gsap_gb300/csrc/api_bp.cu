@@ -1,0 +1,543 @@
+// C ABI of the broadphase (include/gsap.h): handle, scratch ownership and the
+// launch sequence of one call.
+//
+// Replaces the host side of the reference's Sap class
+// (sapDetection/Sap.cpp:12-335).  The reference sizes every launch on the
+// host and reads counts back in between (>= 8 blocking device-to-host
+// copies per Sap::collision, CUDPP plans created per call); here all counts
+// stay on the device, each stage sizes itself from them, and a call is a
+// fixed sequence of launches on the caller's stream (optionally a cached
+// CUDA graph) followed, only when the caller asks for host counts, by one
+// small read of the control block.
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/gsap.h"
+#include "../../include/gsap_debug.h"
+#include "api_internal.h"
+#include "internal.cuh"
+#include "scene_math.cuh"
+
+using namespace gsap;
+
+// ------------------------------------------------------------------ errors
+
+static thread_local std::string g_err;
+
+static gsap_status fail(gsap_status st, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return st;
+}
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return fail(GSAP_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                        __FILE__, __LINE__);                                                  \
+    } while (0)
+
+extern "C" const char* gsap_last_error(void) { return g_err.c_str(); }
+
+gsap_status gsap::set_error(gsap_status st, const char* msg) { return fail(st, "%s", msg); }
+
+namespace gsap {
+int sm_count() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+}  // namespace gsap
+
+extern "C" void gsap_config_default(gsap_config* c) {
+    if (!c) return;
+    memset(c, 0, sizeof(*c));
+    c->mode = GSAP_MODE_AABB;
+    c->axis_mode = GSAP_AXIS_PCA;
+    c->max_scenes = 1;
+    c->entry_factor = 8;
+    c->pair_factor = 16;
+    c->sort_bits = 32;
+    c->cell_factor = 1.5f;
+    c->spin_limit = kDefaultSpin;
+}
+
+// ------------------------------------------------------------------ handle
+
+struct GraphKey {
+    const void *mn, *mx, *off, *pairs, *dcount, *entries;
+    uint32_t n, S, flags, mode, both;
+    uint64_t cap, ecap;
+    bool operator==(const GraphKey& o) const { return memcmp(this, &o, sizeof(*this)) == 0; }
+};
+
+struct gsap_sap {
+    gsap_config cfg;
+    BpScratch s;
+    int device;
+    uint32_t* h_ctrl;   // pinned copy of the head of the control block
+    cudaStream_t cap_stream;
+    cudaGraphExec_t gexec;
+    GraphKey gkey;
+    bool has_graph;
+    bool timing;
+    cudaEvent_t ev[8];
+    float stage_ms[6];
+    int nstages;
+};
+
+static void free_scratch(gsap_sap* h) {
+    BpScratch& s = h->s;
+    void* ptrs[] = {s.ctrl, s.scenes, s.partials, s.scene_done, s.work_start, s.objcell, s.objscene,
+                    s.keys[0], s.keys[1], s.vals[0], s.vals[1], s.status, s.rowcnt, s.rowoff, s.tmp_pairs};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (h->h_ctrl) cudaFreeHost(h->h_ctrl);
+    if (h->has_graph) cudaGraphExecDestroy(h->gexec);
+    if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
+    for (auto& e : h->ev)
+        if (e) cudaEventDestroy(e);
+}
+
+extern "C" gsap_sap* gsap_sap_create(uint32_t max_n, const gsap_config* cfg) {
+    gsap_config c;
+    gsap_config_default(&c);
+    if (cfg) c = *cfg;
+    if (c.max_scenes == 0) c.max_scenes = 1;
+    if (c.entry_factor == 0) c.entry_factor = 8;
+    if (c.pair_factor == 0) c.pair_factor = 16;
+    if (c.sort_bits == 0) c.sort_bits = 32;
+    if (c.sort_bits != 24 && c.sort_bits != 32) { fail(GSAP_ERR_INVALID, "sort_bits must be 24 or 32"); return nullptr; }
+    if (c.cell_factor <= 0.f) c.cell_factor = 1.5f;
+    if (c.spin_limit == 0) c.spin_limit = kDefaultSpin;
+    if (max_n == 0) max_n = 1;
+    uint64_t ecap = (uint64_t)c.entry_factor * max_n + 4096;
+    if (ecap >= (1ull << 30)) { fail(GSAP_ERR_INVALID, "entry capacity %llu exceeds 2^30", (unsigned long long)ecap); return nullptr; }
+    gsap_sap* h = new gsap_sap();
+    memset(h, 0, sizeof(*h));
+    h->cfg = c;
+    cudaGetDevice(&h->device);
+    BpScratch& s = h->s;
+    s.max_n = max_n;
+    s.max_scenes = c.max_scenes;
+    s.max_work = (max_n + kChunk - 1) / kChunk + c.max_scenes + 1;
+    s.entry_cap = ecap;
+    s.pair_cap_internal = (uint64_t)c.pair_factor * max_n + 4096;
+    uint64_t tiles = (ecap + kSortTile - 1) / kSortTile + 1;
+    s.status_words = tiles * 256 + (max_n / 2048 + 2);
+    bool ok = true;
+    auto A = [&](void** p, size_t bytes) {
+        if (!ok) return;
+        if (cudaMalloc(p, bytes) != cudaSuccess) { ok = false; return; }
+        if (cudaMemset(*p, 0, bytes) != cudaSuccess) ok = false;
+    };
+    A((void**)&s.ctrl, sizeof(Ctrl));
+    A((void**)&s.scenes, sizeof(Scene) * c.max_scenes);
+    A((void**)&s.partials, sizeof(PcaPartial) * s.max_work);
+    A((void**)&s.scene_done, 4ull * c.max_scenes);
+    A((void**)&s.work_start, 4ull * (c.max_scenes + 1));
+    A((void**)&s.objcell, 4ull * max_n);
+    if (c.max_scenes > 1) A((void**)&s.objscene, 4ull * max_n);
+    for (int k = 0; k < 2; ++k) {
+        A((void**)&s.keys[k], 4ull * ecap);
+        A((void**)&s.vals[k], 4ull * ecap);
+    }
+    A((void**)&s.status, 8ull * s.status_words);
+    A((void**)&s.rowcnt, 4ull * (max_n + 1));
+    A((void**)&s.rowoff, 4ull * (max_n + 1));
+    A((void**)&s.tmp_pairs, 8ull * s.pair_cap_internal);
+    if (ok && cudaMallocHost((void**)&h->h_ctrl, 64) != cudaSuccess) ok = false;
+    if (ok && cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking) != cudaSuccess) ok = false;
+    for (auto& e : h->ev)
+        if (ok && cudaEventCreate(&e) != cudaSuccess) ok = false;
+    if (!ok) {
+        cudaError_t e = cudaGetLastError();
+        fail(GSAP_ERR_CUDA, "gsap_sap_create: allocation failed (%s)", cudaGetErrorString(e));
+        free_scratch(h);
+        delete h;
+        return nullptr;
+    }
+    return h;
+}
+
+extern "C" void gsap_sap_destroy(gsap_sap* h) {
+    if (!h) return;
+    free_scratch(h);
+    delete h;
+}
+
+extern "C" void gsap_sap_enable_timing(gsap_sap* h, int enable) {
+    if (h) h->timing = enable != 0;
+}
+
+extern "C" int gsap_sap_stage_times(gsap_sap* h, float* out, int max_stages) {
+    if (!h || !out) return 0;
+    int k = 0;
+    for (; k < h->nstages && k < max_stages; ++k) out[k] = h->stage_ms[k];
+    return k;
+}
+
+// ---------------------------------------------------------------- pipeline
+
+struct Call {
+    const float4 *mn, *mx;
+    const uint32_t* off;
+    uint32_t n, S;
+    int mode;
+    uint2* pairs;
+    uint64_t cap;
+    uint64_t* d_count;
+    int32_t* entries;   // both-direction format: pairEntries output
+    uint64_t ecap;
+    uint32_t flags;
+    int both;           // 1: Sap::collision format
+};
+
+static gsap_status record(gsap_sap* h, const Call& c, cudaStream_t st, bool timed) {
+    BpScratch& s = h->s;
+    BpArgs a;
+    a.mn = c.mn;
+    a.mx = c.mx;
+    a.scene_off = c.off;
+    a.n = c.n;
+    a.num_scenes = c.S;
+    a.num_work = (c.n + kChunk - 1) / kChunk + (c.off ? c.S : 1);
+    a.mode = c.mode;
+    a.axis_mode = (int)h->cfg.axis_mode;
+    a.key_bits = h->cfg.sort_bits;
+    a.cell_factor = h->cfg.cell_factor;
+    a.spin_limit = h->cfg.spin_limit;
+    const int passes = (int)(a.key_bits / 8);
+    int ev = 0;
+    auto mark = [&]() {
+        if (timed) cudaEventRecord(h->ev[ev++], st);
+    };
+    mark();
+    if (c.off) CK(launch_plan(s, a, st));
+    CK(launch_pca(s, a, st));
+    mark();
+    CK(launch_project(s, a, passes, st));
+    mark();
+    const uint32_t* count = &s.ctrl->entry_count;
+    int src = 0;
+    for (int p = 0; p < passes; ++p) {
+        CK(launch_sort_pass(s, p, passes, s.keys[src], s.vals[src], s.keys[src ^ 1], s.vals[src ^ 1], count,
+                            s.entry_cap, a.spin_limit, st));
+        src ^= 1;
+    }
+    mark();
+    const bool canon = (c.flags & GSAP_FLAG_SORTED) || c.both;
+    uint2* sweep_out = canon ? (uint2*)s.tmp_pairs : c.pairs;
+    uint64_t sweep_cap = canon ? s.pair_cap_internal : c.cap;
+    CK(launch_sweep(s, a, s.keys[src], s.vals[src], sweep_out, sweep_cap, canon ? (c.both ? 2 : 1) : 0, st));
+    mark();
+    if (canon) {
+        CK(launch_canonical(s, c.n, (const uint2*)s.tmp_pairs, s.pair_cap_internal, c.pairs, c.cap, c.both,
+                            c.entries, c.ecap, a.spin_limit, st));
+        mark();
+    }
+    if (c.d_count) CK(cudaMemcpyAsync(c.d_count, &s.ctrl->pair_count, 8, cudaMemcpyDeviceToDevice, st));
+    if (timed) h->nstages = ev - 1;
+    return GSAP_OK;
+}
+
+static gsap_status run(gsap_sap* h, const Call& c, cudaStream_t st) {
+    int dev = -1;
+    cudaGetDevice(&dev);
+    if (dev != h->device) return fail(GSAP_ERR_INVALID, "handle was created on device %d, current is %d", h->device, dev);
+    const bool use_graph = (c.flags & GSAP_FLAG_GRAPH) && !h->timing;
+    if (!use_graph) return record(h, c, st, h->timing);
+    GraphKey k;
+    memset(&k, 0, sizeof(k));
+    k.mn = c.mn; k.mx = c.mx; k.off = c.off; k.pairs = c.pairs; k.dcount = c.d_count; k.entries = c.entries;
+    k.n = c.n; k.S = c.S; k.flags = c.flags; k.mode = (uint32_t)c.mode; k.both = (uint32_t)c.both;
+    k.cap = c.cap; k.ecap = c.ecap;
+    if (!h->has_graph || !(h->gkey == k)) {
+        if (h->has_graph) {
+            cudaGraphExecDestroy(h->gexec);
+            h->has_graph = false;
+        }
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal));
+        gsap_status r = record(h, c, h->cap_stream, false);
+        cudaError_t e = cudaStreamEndCapture(h->cap_stream, &g);
+        if (r != GSAP_OK) return r;
+        if (e != cudaSuccess) return fail(GSAP_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&h->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(GSAP_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+        h->has_graph = true;
+        h->gkey = k;
+    }
+    CK(cudaGraphLaunch(h->gexec, st));
+    return GSAP_OK;
+}
+
+// Reads error word and pair count (synchronizes), clears the error word.
+static gsap_status finish(gsap_sap* h, cudaStream_t st, uint64_t* count_out, uint64_t cap) {
+    CK(cudaMemcpyAsync(h->h_ctrl, h->s.ctrl, 24, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (h->timing)
+        for (int k = 0; k < h->nstages; ++k) cudaEventElapsedTime(&h->stage_ms[k], h->ev[k], h->ev[k + 1]);
+    uint32_t err = h->h_ctrl[0];
+    uint64_t cnt;
+    memcpy(&cnt, (char*)h->h_ctrl + 16, 8);
+    if (count_out) *count_out = cnt;
+    if (err) {
+        CK(cudaMemsetAsync(&h->s.ctrl->error, 0, 4, st));
+        CK(cudaStreamSynchronize(st));
+        if (err & kErrTimeout) return fail(GSAP_ERR_DEVICE_TIMEOUT, "a device-side wait exceeded its iteration cap");
+        if (err & kErrNonFinite) return fail(GSAP_ERR_NONFINITE, "NaN or Inf in the input bounds");
+        if (err & kErrEntryCap) return fail(GSAP_ERR_CAPACITY, "sweep entries exceeded the handle's capacity (raise entry_factor)");
+        if (err & kErrCellRange) return fail(GSAP_ERR_CAPACITY, "too many sweep cells for the key width");
+        if (err & kErrPairCap) return fail(GSAP_ERR_CAPACITY, "pairs exceeded an output capacity");
+        return fail(GSAP_ERR_CUDA, "device error word 0x%x", err);
+    }
+    if (cnt > cap) return fail(GSAP_ERR_CAPACITY, "%llu pairs exceed the capacity %llu", (unsigned long long)cnt, (unsigned long long)cap);
+    return GSAP_OK;
+}
+
+static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+static gsap_status validate(gsap_sap* h, const float* mn, const float* mx, uint32_t n, int mode, const void* pairs,
+                            uint32_t S) {
+    if (!h) return fail(GSAP_ERR_INVALID, "null handle");
+    if (n > h->s.max_n) return fail(GSAP_ERR_CAPACITY, "n = %u exceeds the handle's max_n = %u", n, h->s.max_n);
+    if (S > h->s.max_scenes) return fail(GSAP_ERR_CAPACITY, "%u scenes exceed max_scenes = %u", S, h->s.max_scenes);
+    if (n > 0 && (!mn || !aligned16(mn))) return fail(GSAP_ERR_INVALID, "bounds pointer null or not 16-byte aligned");
+    if (n > 0 && mode == GSAP_MODE_AABB && (!mx || !aligned16(mx)))
+        return fail(GSAP_ERR_INVALID, "max-bounds pointer null or not 16-byte aligned");
+    if (n > 1 && !pairs) return fail(GSAP_ERR_INVALID, "null pair output");
+    if (pairs && ((uintptr_t)pairs & 7u)) return fail(GSAP_ERR_INVALID, "pair output not 8-byte aligned");
+    return GSAP_OK;
+}
+
+static gsap_status broadphase(gsap_sap* h, const float* d_min, const float* d_max, const uint32_t* off,
+                              uint32_t S, uint32_t n, uint32_t* d_pairs, uint64_t cap, uint64_t* d_count,
+                              uint64_t* h_count, uint32_t flags, void* stream) {
+    int mode = (int)h->cfg.mode;
+    gsap_status v = validate(h, d_min, d_max, n, mode, d_pairs, S);
+    if (v != GSAP_OK) return v;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n < 2 && !off) {
+        if (d_count) CK(cudaMemsetAsync(d_count, 0, 8, st));
+        if (h_count) *h_count = 0;
+        return GSAP_OK;
+    }
+    Call c;
+    memset(&c, 0, sizeof(c));
+    c.mn = (const float4*)d_min;
+    c.mx = mode == GSAP_MODE_AABB ? (const float4*)d_max : nullptr;
+    c.off = off;
+    c.n = n;
+    c.S = off ? S : 1;
+    c.mode = mode;
+    c.pairs = (uint2*)d_pairs;
+    c.cap = cap;
+    c.d_count = d_count;
+    c.flags = flags;
+    gsap_status r = run(h, c, st);
+    if (r != GSAP_OK) return r;
+    // sorted output goes through the internal pair buffer first
+    uint64_t eff = (flags & GSAP_FLAG_SORTED) ? (cap < h->s.pair_cap_internal ? cap : h->s.pair_cap_internal) : cap;
+    if (h_count) return finish(h, st, h_count, eff);
+    return GSAP_OK;
+}
+
+extern "C" gsap_status gsap_broadphase_aabb(gsap_sap* h, const float* d_min, const float* d_max, uint32_t n,
+                                            uint32_t* d_pairs, uint64_t pair_cap, uint64_t* d_count,
+                                            uint64_t* h_count, uint32_t flags, void* stream) {
+    return broadphase(h, d_min, d_max, nullptr, 1, n, d_pairs, pair_cap, d_count, h_count, flags, stream);
+}
+
+extern "C" gsap_status gsap_broadphase_batched(gsap_sap* h, const float* d_min, const float* d_max,
+                                               const uint32_t* d_scene_offsets, uint32_t num_scenes, uint32_t n,
+                                               uint32_t* d_pairs, uint64_t pair_cap, uint64_t* d_count,
+                                               uint64_t* h_count, uint32_t flags, void* stream) {
+    if (!d_scene_offsets || num_scenes == 0) return fail(GSAP_ERR_INVALID, "batched call needs scene offsets");
+    if (!h) return fail(GSAP_ERR_INVALID, "null handle");
+    if (h->s.max_scenes < 2 && num_scenes > 1)
+        return fail(GSAP_ERR_INVALID, "handle created with max_scenes = %u", h->s.max_scenes);
+    if (n == 0) {
+        if (d_count) CK(cudaMemsetAsync(d_count, 0, 8, (cudaStream_t)stream));
+        if (h_count) *h_count = 0;
+        return GSAP_OK;
+    }
+    return broadphase(h, d_min, d_max, d_scene_offsets, num_scenes, n, d_pairs, pair_cap, d_count, h_count, flags,
+                      stream);
+}
+
+extern "C" gsap_status gsap_sap_collision(gsap_sap* h, float spacing, const float* d_spheres, uint32_t n,
+                                          int32_t* d_pairs, int32_t* d_pair_entries, int32_t* h_num_pairs,
+                                          int32_t* h_num_entries, uint64_t pair_cap, uint64_t entry_cap,
+                                          void* stream) {
+    (void)spacing;
+    gsap_status v = validate(h, d_spheres, nullptr, n, GSAP_MODE_SPHERE, d_pairs, 1);
+    if (v != GSAP_OK) return v;
+    if (!d_pair_entries && n > 1) return fail(GSAP_ERR_INVALID, "null pairEntries output");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n < 2) {
+        if (h_num_pairs) *h_num_pairs = 0;
+        if (h_num_entries) *h_num_entries = 0;
+        return GSAP_OK;
+    }
+    Call c;
+    memset(&c, 0, sizeof(c));
+    c.mn = (const float4*)d_spheres;
+    c.n = n;
+    c.S = 1;
+    c.mode = GSAP_MODE_SPHERE;
+    c.pairs = (uint2*)d_pairs;
+    c.cap = pair_cap;
+    c.entries = d_pair_entries;
+    c.ecap = entry_cap;
+    c.both = 1;
+    gsap_status r = run(h, c, st);
+    if (r != GSAP_OK) return r;
+    uint64_t np = 0;
+    uint64_t half = pair_cap / 2;
+    r = finish(h, st, &np, half < h->s.pair_cap_internal ? half : h->s.pair_cap_internal);
+    uint32_t ne = 0;
+    CK(cudaMemcpyAsync(&ne, &h->s.ctrl->scan_total, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (h_num_pairs) *h_num_pairs = (int32_t)(2 * np);
+    if (h_num_entries) *h_num_entries = (int32_t)ne;
+    if (r != GSAP_OK) return r;
+    if (2 * np > pair_cap) return fail(GSAP_ERR_CAPACITY, "%llu pairs exceed the capacity %llu", (unsigned long long)(2 * np), (unsigned long long)pair_cap);
+    if (ne > entry_cap) return fail(GSAP_ERR_CAPACITY, "%u pair entries exceed the capacity %llu", ne, (unsigned long long)entry_cap);
+    return GSAP_OK;
+}
+
+extern "C" gsap_status gsap_sap_check(gsap_sap* h, void* stream) {
+    if (!h) return fail(GSAP_ERR_INVALID, "null handle");
+    return finish(h, (cudaStream_t)stream, nullptr, ~0ull);
+}
+
+extern "C" gsap_status gsap_sap_scene_axes(gsap_sap* h, uint32_t scene, double* out, void* stream) {
+    if (!h || !out) return fail(GSAP_ERR_INVALID, "null argument");
+    if (scene >= h->s.max_scenes) return fail(GSAP_ERR_INVALID, "scene index out of range");
+    Scene sc;
+    CK(cudaMemcpyAsync(&sc, &h->s.scenes[scene], sizeof(Scene), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    CK(cudaStreamSynchronize((cudaStream_t)stream));
+    for (int k = 0; k < 9; ++k) out[k] = sc.axes[k];
+    for (int k = 0; k < 3; ++k) { out[9 + k] = sc.eig[k]; out[12 + k] = sc.mean[k]; }
+    out[15] = sc.G2;
+    out[16] = sc.G3;
+    return GSAP_OK;
+}
+
+extern "C" gsap_status gsap_radix_sort_u32(gsap_sap* h, uint32_t* d_keys, uint32_t* d_vals, uint32_t n,
+                                           uint32_t bits, void* stream) {
+    if (!h || (!d_keys && n)) return fail(GSAP_ERR_INVALID, "null argument");
+    if (n > h->s.entry_cap) return fail(GSAP_ERR_CAPACITY, "n = %u exceeds the sort capacity %llu", n, (unsigned long long)h->s.entry_cap);
+    if (bits == 0 || bits > 32) return fail(GSAP_ERR_INVALID, "bits must be in 1..32");
+    if (n < 2) return GSAP_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    BpScratch& s = h->s;
+    const int passes = (int)((bits + 7) / 8);
+    uint32_t* count = &s.ctrl->sort_n;
+    CK(launch_sort_prep(s, d_keys, count, n, passes, st));
+    uint32_t* vals = d_vals ? d_vals : s.vals[0];
+    if (!d_vals) CK(cudaMemsetAsync(vals, 0, 4ull * n, st));
+    uint32_t* kb[2] = {d_keys, s.keys[1]};
+    uint32_t* vb[2] = {vals, s.vals[1]};
+    int src = 0;
+    for (int p = 0; p < passes; ++p) {
+        CK(launch_sort_pass(s, p, passes, kb[src], vb[src], kb[src ^ 1], vb[src ^ 1], count, n, h->cfg.spin_limit, st));
+        src ^= 1;
+    }
+    if (src) {
+        CK(cudaMemcpyAsync(d_keys, kb[1], 4ull * n, cudaMemcpyDeviceToDevice, st));
+        if (d_vals) CK(cudaMemcpyAsync(d_vals, vb[1], 4ull * n, cudaMemcpyDeviceToDevice, st));
+    }
+    return finish(h, st, nullptr, ~0ull);
+}
+
+// ------------------------------------------------------------ debug hooks
+
+extern "C" int gsap_debug_scene_solve(const double* sums18, const double* hmax3, const double* pilot3, double n,
+                                      uint32_t n_total, uint32_t axis_mode, float cell_factor, uint32_t key_bits,
+                                      uint64_t entry_cap, double* out17) {
+    if (!sums18 || !hmax3 || !pilot3 || !out17) return -1;
+    SceneSums z;
+    for (int k = 0; k < 3; ++k) {
+        z.sd[k] = sums18[k];
+        z.sh[k] = sums18[9 + k];
+        z.hmax[k] = hmax3[k];
+        z.pilot[k] = pilot3[k];
+    }
+    for (int k = 0; k < 6; ++k) {
+        z.sdd[k] = sums18[3 + k];
+        z.shh[k] = sums18[12 + k];
+    }
+    z.n = n;
+    BpArgs a;
+    memset(&a, 0, sizeof(a));
+    a.axis_mode = (int)axis_mode;
+    a.cell_factor = cell_factor;
+    a.key_bits = key_bits;
+    Scene sc;
+    memset(&sc, 0, sizeof(sc));
+    choose_scene(z, a, entry_cap, n_total, sc);
+    for (int k = 0; k < 9; ++k) out17[k] = sc.axes[k];
+    for (int k = 0; k < 3; ++k) { out17[9 + k] = sc.eig[k]; out17[12 + k] = sc.mean[k]; }
+    out17[15] = sc.G2;
+    out17[16] = sc.G3;
+    return 0;
+}
+
+extern "C" int gsap_debug_sizes(uint32_t* out) {
+    if (!out) return -1;
+    out[0] = sizeof(Ctrl);
+    out[1] = sizeof(Scene);
+    out[2] = sizeof(PcaPartial);
+    out[3] = kSortTile;
+    return 0;
+}
+
+gsap_status gsap::bp_both_async(gsap_sap* h, int mode, const float4* mn, const float4* mx, const uint32_t* off,
+                                uint32_t S, uint32_t n, uint2* pairs, uint64_t cap, int32_t* entries,
+                                uint64_t entry_cap, cudaStream_t st, BpDeviceCounts* out) {
+    gsap_status v = validate(h, (const float*)mn, (const float*)mx, n, mode, pairs, off ? S : 1);
+    if (v != GSAP_OK) return v;
+    if (out) {
+        out->num_pairs = &h->s.ctrl->pair_count;
+        out->num_entries = &h->s.ctrl->scan_total;
+        out->rowoff = h->s.rowoff;
+    }
+    Call c;
+    memset(&c, 0, sizeof(c));
+    c.mn = mn;
+    c.mx = mode == GSAP_MODE_AABB ? mx : nullptr;
+    c.off = off;
+    c.n = n;
+    c.S = off ? S : 1;
+    c.mode = mode;
+    c.pairs = pairs;
+    c.cap = cap;
+    c.entries = entries;
+    c.ecap = entry_cap;
+    c.both = 1;
+    if (n < 2 && !off) {
+        // empty list: zero the counts and row offsets the consumers read
+        CK(cudaMemsetAsync(&h->s.ctrl->pair_count, 0, 8, st));
+        CK(cudaMemsetAsync(&h->s.ctrl->scan_total, 0, 4, st));
+        CK(cudaMemsetAsync(h->s.rowoff, 0, 4ull * (n + 1), st));
+        return GSAP_OK;
+    }
+    return record(h, c, st, false);
+}

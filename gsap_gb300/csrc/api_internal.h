@@ -1,0 +1,25 @@
+// C++-only entry points shared between the broadphase and rigid-body C-ABI
+// layers.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/gsap.h"
+
+namespace gsap {
+
+struct BpDeviceCounts {
+    const unsigned long long* num_pairs;  // i<j pairs of the last call (device)
+    const uint32_t* num_entries;          // pairEntries count (device, both-direction format)
+    const uint32_t* rowoff;               // per-object row offsets of the both-direction list (n+1)
+};
+
+// Both-direction canonical pair list (Sap::collision format, any predicate)
+// without any host synchronisation: the counts stay on the device.
+gsap_status bp_both_async(gsap_sap* h, int mode, const float4* mn, const float4* mx, const uint32_t* scene_off,
+                          uint32_t num_scenes, uint32_t n, uint2* pairs, uint64_t cap, int32_t* entries,
+                          uint64_t entry_cap, cudaStream_t st, BpDeviceCounts* out);
+
+gsap_status set_error(gsap_status st, const char* msg);
+
+}  // namespace gsap

@@ -1,0 +1,241 @@
+// Internal declarations shared by the sm_103a kernels and the C-ABI layer.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gsap {
+
+constexpr int kChunk = 4096;          // objects per PCA / projection work item
+constexpr int kThreads = 256;         // threads per CTA of the streaming kernels
+constexpr int kMaxPasses = 4;         // radix passes (8-bit digits, <= 32-bit keys)
+constexpr int kSortItems = 16;        // keys per thread in a onesweep tile
+constexpr int kSortTile = kThreads * kSortItems;
+constexpr uint32_t kDefaultSpin = 1u << 24;
+
+// Sticky device error bits (ctrl->error).
+enum : uint32_t {
+    kErrEntryCap = 1u,     // sweep entries exceeded their capacity
+    kErrPairCap = 2u,      // pairs exceeded the output capacity
+    kErrTimeout = 4u,      // a bounded wait gave up
+    kErrNonFinite = 8u,    // NaN / Inf in the input bounds
+    kErrCellRange = 16u,   // internal: grid wider than 65535 cells per axis
+};
+
+// Look-back status word: [63:32] tag, [31:30] flag, [29:0] value.
+constexpr uint64_t kFlagAgg = 1ull << 30;
+constexpr uint64_t kFlagPrefix = 2ull << 30;
+constexpr uint32_t kValMask = (1u << 30) - 1u;
+
+// Control block: counters shared by the stages of one call.  Counters that a
+// stage consumes are reset by the stage that runs before it (the PCA
+// kernel's last CTA resets the projection/sort/sweep counters), or by their
+// own last user (per-scene PCA counters), so that no memset runs per call.
+struct Ctrl {
+    uint32_t error;
+    uint32_t epoch;           // ++ once per pipeline run; tags look-back words
+    uint32_t scenes_done;     // PCA: completed scenes (self-resetting)
+    uint32_t entry_count;     // projection output count
+    unsigned long long pair_count;
+    uint32_t tile_ctr[kMaxPasses + 4];
+    uint32_t sweep_ctr;
+    uint32_t key_bits;        // total radix key width of this run
+    uint32_t qbits;           // low bits of the key holding the quantised lower bound
+    uint32_t total_buckets;
+    uint32_t scan_total;      // total of the last look-back scan
+    uint32_t scan_ctr;        // tile counter of the look-back scan
+    uint32_t sort_n;          // key count of a standalone sort
+    uint32_t pad;
+    uint32_t hist[kMaxPasses][256];
+};
+
+// Per-scene parameters written by the PCA kernel.
+struct Scene {
+    float u[9];          // sweep axis u1 then secondary axes u2, u3 (rows)
+    float q_org, q_range; // lower-bound quantisation: q = (x - q_org) * (2^Q / q_range)
+    float c2_org, c2_inv; // cell index on u2: floor((x - c2_org) * c2_inv), clamped
+    float c3_org, c3_inv;
+    uint32_t G2, G3;      // cells per secondary axis
+    uint32_t bucket_base; // first global bucket id of this scene
+    uint32_t n;           // objects in the scene
+    uint32_t pad[2];
+    double eig[3];        // eigenvalues, descending
+    double mean[3];       // centre mean
+    double axes[9];       // FP64 axes (rows)
+};
+
+// PCA partial sums of one work item: 18 (hi, lo) compensated FP32 pairs
+// (sum d, sum d d^T, sum h, sum h h^T with d = centre - pilot, h =
+// |half extent|), then max |h| per axis.
+constexpr int kPcaQ = 18;
+struct PcaPartial {
+    float hi[kPcaQ];
+    float lo[kPcaQ];
+    float hmax[3];
+    float pad;
+};
+
+// Device scratch of a broadphase handle.
+struct BpScratch {
+    Ctrl* ctrl;
+    Scene* scenes;
+    PcaPartial* partials;
+    uint32_t* scene_done;      // per-scene PCA completion counters
+    uint32_t* work_start;      // per-scene first work item (S+1), batched plan
+    uint32_t* objcell;         // per object: (c2lo << 16) | c3lo
+    uint32_t* objscene;        // per object scene id (batched only)
+    uint32_t* keys[2];
+    uint32_t* vals[2];
+    uint64_t* status;          // look-back words
+    uint32_t* rowcnt;          // per object pair counts (canonical output)
+    uint32_t* rowoff;          // exclusive offsets, n+1
+    uint32_t* tmp_pairs;       // unsorted pairs before canonicalisation
+    uint64_t entry_cap;
+    uint64_t pair_cap_internal;
+    uint64_t status_words;
+    uint32_t max_n;
+    uint32_t max_scenes;
+    uint32_t max_work;
+};
+
+struct BpArgs {
+    const float4* mn;          // AABB min (or spheres)
+    const float4* mx;          // AABB max (nullptr in sphere mode)
+    const uint32_t* scene_off; // device S+1 offsets (nullptr: one scene)
+    uint32_t n;
+    uint32_t num_scenes;
+    uint32_t num_work;         // upper bound of work items launched
+    int mode;                  // 0 AABB, 1 sphere
+    int axis_mode;             // 0 PCA, 1 reference axis
+    uint32_t key_bits;         // 24 or 32
+    float cell_factor;
+    uint32_t spin_limit;
+};
+
+// ---------------------------------------------------------------- launches
+// Each returns cudaGetLastError() of its launch.
+cudaError_t launch_plan(const BpScratch& s, const BpArgs& a, cudaStream_t st);
+cudaError_t launch_pca(const BpScratch& s, const BpArgs& a, cudaStream_t st);
+cudaError_t launch_project(const BpScratch& s, const BpArgs& a, int passes, cudaStream_t st);
+cudaError_t launch_sort_pass(const BpScratch& s, int pass, int passes, const uint32_t* kin,
+                             const uint32_t* vin, uint32_t* kout, uint32_t* vout,
+                             const uint32_t* count_ptr, uint64_t cap, uint32_t spin, cudaStream_t st);
+cudaError_t launch_sort_prep(const BpScratch& s, const uint32_t* keys, const uint32_t* count_ptr,
+                             uint32_t n, int passes, cudaStream_t st);
+cudaError_t launch_sweep(const BpScratch& s, const BpArgs& a, const uint32_t* keys, const uint32_t* vals,
+                         uint2* pairs, uint64_t pair_cap, int count_rows, cudaStream_t st);
+cudaError_t launch_canonical(const BpScratch& s, uint32_t n, const uint2* in_pairs, uint64_t in_cap,
+                             uint2* out_pairs, uint64_t out_cap, int both, int32_t* entries,
+                             uint64_t entry_cap, uint32_t spin, cudaStream_t st);
+int sm_count();
+
+// ------------------------------------------------------------ device helpers
+#ifdef __CUDACC__
+__device__ __forceinline__ uint64_t ld_acquire_u64(const uint64_t* p) {
+    uint64_t v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u64(uint64_t* p, uint64_t v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+__device__ __forceinline__ uint64_t lb_word(uint32_t tag, uint64_t flag, uint32_t val) {
+    return ((uint64_t)tag << 32) | flag | (uint64_t)(val & kValMask);
+}
+
+// Bounded decoupled look-back over the tiles before `tile` for column `col`
+// of a status table with `cols` columns.  Returns the exclusive prefix; on
+// timeout sets kErrTimeout and returns what it has (the caller still
+// publishes, so no later tile can wait forever).
+__device__ __forceinline__ uint32_t lookback(uint64_t* status, uint32_t tile, uint32_t col, uint32_t cols,
+                                             uint32_t tag, uint32_t spin_limit, uint32_t* err) {
+    uint32_t excl = 0;
+    int64_t j = (int64_t)tile - 1;
+    while (j >= 0) {
+        uint64_t v;
+        uint32_t spins = 0;
+        while (true) {
+            v = ld_acquire_u64(status + (uint64_t)j * cols + col);
+            if ((uint32_t)(v >> 32) == tag && (v & (kFlagAgg | kFlagPrefix))) break;
+            if (++spins > spin_limit) {
+                atomicOr(err, kErrTimeout);
+                return excl;
+            }
+            if (spins > 64) __nanosleep(64);
+        }
+        excl += (uint32_t)(v & kValMask);
+        if (v & kFlagPrefix) break;
+        --j;
+    }
+    return excl;
+}
+
+// Error-free transformation a + b = s + e (Knuth two-sum).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// Compensated accumulation (hi, lo) += x.
+__device__ __forceinline__ void kahan_add(float& hi, float& lo, float x) {
+    float s, e;
+    two_sum(hi, x, s, e);
+    hi = s;
+    lo = __fadd_rn(lo, e);
+}
+// Merge two compensated sums.
+__device__ __forceinline__ void kahan_merge(float& hi, float& lo, float hi2, float lo2) {
+    float s, e;
+    two_sum(hi, hi2, s, e);
+    hi = s;
+    lo = __fadd_rn(__fadd_rn(lo, lo2), e);
+}
+#endif
+
+// ------------------------------------------------------------- work plan
+#ifdef __CUDACC__
+
+__device__ __forceinline__ uint32_t scene_begin(const BpArgs& A, uint32_t s) {
+    return A.scene_off ? A.scene_off[s] : 0u;
+}
+__device__ __forceinline__ uint32_t scene_end(const BpArgs& A, uint32_t s) {
+    return A.scene_off ? A.scene_off[s + 1] : A.n;
+}
+__device__ __forceinline__ uint32_t work_items(uint32_t n_s) {
+    return n_s == 0 ? 1u : (n_s + kChunk - 1) / kChunk;
+}
+
+// Work item -> (scene, object range, first work item of the scene, count).
+__device__ __forceinline__ bool map_work(uint32_t w, const BpScratch& S, const BpArgs& A, uint32_t& scene,
+                                         uint32_t& b, uint32_t& e, uint32_t& wfirst, uint32_t& nw) {
+    if (!A.scene_off) {
+        nw = work_items(A.n);
+        if (w >= nw) return false;
+        scene = 0;
+        wfirst = 0;
+        b = w * kChunk;
+        e = min(A.n, b + kChunk);
+        return true;
+    }
+    if (w >= S.work_start[A.num_scenes]) return false;
+    uint32_t lo = 0, hi = A.num_scenes;  // last s with work_start[s] <= w
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (S.work_start[mid] <= w) lo = mid;
+        else hi = mid;
+    }
+    scene = lo;
+    wfirst = S.work_start[lo];
+    nw = S.work_start[lo + 1] - wfirst;
+    uint32_t sb = A.scene_off[lo], se = A.scene_off[lo + 1];
+    b = sb + (w - wfirst) * kChunk;
+    e = min(se, b + kChunk);
+    return true;
+}
+#endif
+
+}  // namespace gsap

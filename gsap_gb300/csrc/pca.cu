@@ -1,0 +1,248 @@
+// K1: segmented PCA of the object centres.
+//
+// Replaces the reference's Sap::Deviation / reduceExt / calDev / reduce6 /
+// axisVecMultiple chain (sapDetection/Sap.cpp:148-209,
+// sapDetection/SapKernel.cu:1342-1403, :63-97): there, three separate
+// tree reductions over float4 arrays (the covariance rows pre-divided by n
+// and written to two 16n-byte temporaries) feed a <<<1,1>>> kernel that picks
+// the coordinate axis of largest variance.  Here one pass over the input
+// accumulates compensated (two-sum) FP32 sums of d = c - pilot, d d^T, h and
+// h h^T per 4096-object work item; the last work item of each scene combines
+// the partials in FP64 (fixed order: deterministic), solves the 3x3
+// eigenproblem by cyclic Jacobi in FP64 and chooses the sweep grid; the last
+// scene resets the counters of the later stages.
+#include "internal.cuh"
+#include "scene_math.cuh"
+#include <math.h>
+
+namespace gsap {
+
+// Batched plan: first work item of every scene (one CTA, sequential scan in
+// 1024-scene blocks).
+__global__ void __launch_bounds__(1024) k_plan(BpScratch S, BpArgs A) {
+    __shared__ uint32_t s_tot[32];
+    __shared__ uint32_t s_carry;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (uint32_t base = 0; base < A.num_scenes; base += 1024) {
+        uint32_t s = base + threadIdx.x;
+        uint32_t v = s < A.num_scenes ? work_items(A.scene_off[s + 1] - A.scene_off[s]) : 0u;
+        uint32_t x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        if (lane == 31) s_tot[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            uint32_t t = s_tot[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+                if (lane >= (uint32_t)o) t += y;
+            }
+            s_tot[lane] = t;
+        }
+        __syncthreads();
+        uint32_t excl = s_carry + (wid ? s_tot[wid - 1] : 0u) + x - v;
+        if (s < A.num_scenes) S.work_start[s] = excl;
+        __syncthreads();
+        if (threadIdx.x == 1023) s_carry = excl + v;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) S.work_start[A.num_scenes] = s_carry;
+}
+
+// ---------------------------------------------------------------- K1
+
+__global__ void __launch_bounds__(kThreads) k_pca(BpScratch S, BpArgs A, uint64_t entry_cap) {
+    __shared__ float s_red[kThreads / 32][2 * kPcaQ + 3];
+    __shared__ double s_dred[kThreads / 32][kPcaQ + 3];
+    __shared__ uint32_t s_flag;
+    __shared__ double s_pilot[3];
+    const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    uint32_t scene, b, e, wfirst, nw;
+    if (!map_work(blockIdx.x, S, A, scene, b, e, wfirst, nw)) return;
+    const uint32_t sb = scene_begin(A, scene), se = scene_end(A, scene);
+
+    // pilot = centre of the scene's first object (shift against cancellation)
+    float px = 0.f, py = 0.f, pz = 0.f;
+    if (se > sb) {
+        float4 a = A.mn[sb];
+        if (A.mode == 0) {
+            float4 c = A.mx[sb];
+            px = 0.5f * (a.x + c.x); py = 0.5f * (a.y + c.y); pz = 0.5f * (a.z + c.z);
+        } else {
+            px = a.x; py = a.y; pz = a.z;
+        }
+        if (!isfinite(px) || !isfinite(py) || !isfinite(pz)) { px = py = pz = 0.f; }
+    }
+    float hi[kPcaQ], lo[kPcaQ], hm[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < kPcaQ; ++q) { hi[q] = 0.f; lo[q] = 0.f; }
+    bool bad = false;
+    for (uint32_t i = b + tid; i < e; i += kThreads) {
+        float4 a = A.mn[i];
+        float cx, cy, cz, hx, hy, hz;
+        if (A.mode == 0) {
+            float4 c = A.mx[i];
+            cx = 0.5f * (a.x + c.x); cy = 0.5f * (a.y + c.y); cz = 0.5f * (a.z + c.z);
+            hx = 0.5f * fabsf(c.x - a.x); hy = 0.5f * fabsf(c.y - a.y); hz = 0.5f * fabsf(c.z - a.z);
+        } else {
+            cx = a.x; cy = a.y; cz = a.z;
+            hx = hy = hz = fabsf(a.w);
+        }
+        if (!(isfinite(cx) && isfinite(cy) && isfinite(cz) && isfinite(hx) && isfinite(hy) && isfinite(hz))) {
+            bad = true;
+            continue;
+        }
+        float dx = cx - px, dy = cy - py, dz = cz - pz;
+        float v[kPcaQ] = {dx, dy, dz, dx * dx, dx * dy, dx * dz, dy * dy, dy * dz, dz * dz,
+                          hx, hy, hz, hx * hx, hx * hy, hx * hz, hy * hy, hy * hz, hz * hz};
+#pragma unroll
+        for (int q = 0; q < kPcaQ; ++q) kahan_add(hi[q], lo[q], v[q]);
+        hm[0] = fmaxf(hm[0], hx); hm[1] = fmaxf(hm[1], hy); hm[2] = fmaxf(hm[2], hz);
+    }
+    if (bad) atomicOr(&S.ctrl->error, kErrNonFinite);
+    // warp, then CTA, compensated reduction
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int q = 0; q < kPcaQ; ++q) {
+            float h2 = __shfl_down_sync(0xffffffffu, hi[q], o);
+            float l2 = __shfl_down_sync(0xffffffffu, lo[q], o);
+            kahan_merge(hi[q], lo[q], h2, l2);
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) hm[k] = fmaxf(hm[k], __shfl_down_sync(0xffffffffu, hm[k], o));
+    }
+    if (lane == 0) {
+        for (int q = 0; q < kPcaQ; ++q) { s_red[wid][q] = hi[q]; s_red[wid][kPcaQ + q] = lo[q]; }
+        for (int k = 0; k < 3; ++k) s_red[wid][2 * kPcaQ + k] = hm[k];
+    }
+    __syncthreads();
+    if (tid < kPcaQ) {
+        float h = s_red[0][tid], l = s_red[0][kPcaQ + tid];
+        for (int w = 1; w < kThreads / 32; ++w) kahan_merge(h, l, s_red[w][tid], s_red[w][kPcaQ + tid]);
+        S.partials[blockIdx.x].hi[tid] = h;
+        S.partials[blockIdx.x].lo[tid] = l;
+    } else if (tid < kPcaQ + 3) {
+        int k = tid - kPcaQ;
+        float m = s_red[0][2 * kPcaQ + k];
+        for (int w = 1; w < kThreads / 32; ++w) m = fmaxf(m, s_red[w][2 * kPcaQ + k]);
+        S.partials[blockIdx.x].hmax[k] = m;
+    }
+    // last work item of the scene combines
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t old = atomicAdd(&S.scene_done[scene], 1u);
+        s_flag = (old == nw - 1) ? 1u : 0u;
+        s_pilot[0] = px; s_pilot[1] = py; s_pilot[2] = pz;
+    }
+    __syncthreads();
+    if (!s_flag) return;
+    __threadfence();
+    // FP64 combine of the scene's partials: thread t takes items t, t+256, ...
+    double acc[kPcaQ + 3];
+#pragma unroll
+    for (int q = 0; q < kPcaQ + 3; ++q) acc[q] = 0.0;
+    for (uint32_t k = tid; k < nw; k += kThreads) {
+        const PcaPartial* P = &S.partials[wfirst + k];
+#pragma unroll
+        for (int q = 0; q < kPcaQ; ++q) acc[q] += (double)__ldcg(&P->hi[q]) + (double)__ldcg(&P->lo[q]);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) acc[kPcaQ + q] = fmax(acc[kPcaQ + q], (double)__ldcg(&P->hmax[q]));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int q = 0; q < kPcaQ; ++q) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], o);
+#pragma unroll
+        for (int q = kPcaQ; q < kPcaQ + 3; ++q) acc[q] = fmax(acc[q], __shfl_down_sync(0xffffffffu, acc[q], o));
+    }
+    if (lane == 0)
+        for (int q = 0; q < kPcaQ + 3; ++q) s_dred[wid][q] = acc[q];
+    __syncthreads();
+    if (tid == 0) {
+        SceneSums z;
+        double t[kPcaQ + 3];
+        for (int q = 0; q < kPcaQ + 3; ++q) {
+            double v = s_dred[0][q];
+            for (int w = 1; w < kThreads / 32; ++w)
+                v = (q < kPcaQ) ? v + s_dred[w][q] : fmax(v, s_dred[w][q]);
+            t[q] = v;
+        }
+        for (int k = 0; k < 3; ++k) { z.sd[k] = t[k]; z.sh[k] = t[9 + k]; z.hmax[k] = t[kPcaQ + k]; }
+        for (int k = 0; k < 6; ++k) { z.sdd[k] = t[3 + k]; z.shh[k] = t[12 + k]; }
+        for (int k = 0; k < 3; ++k) z.pilot[k] = s_pilot[k];
+        z.n = (double)(se - sb);
+        Scene sc;
+        choose_scene(z, A, entry_cap, A.n, sc);
+        S.scenes[scene] = sc;
+        S.scene_done[scene] = 0u;  // self-reset for the next call
+        __threadfence();
+        uint32_t old = atomicAdd(&S.ctrl->scenes_done, 1u);
+        s_flag = (old == A.num_scenes - 1) ? 2u : 0u;
+    }
+    __syncthreads();
+    if (s_flag != 2u) return;
+    __threadfence();
+    // Last scene: global bucket bases, key layout, and counter reset.
+    __shared__ uint32_t s_wsum[kThreads / 32];
+    __shared__ uint32_t s_carry;
+    if (tid == 0) s_carry = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < A.num_scenes; base += kThreads) {
+        uint32_t s = base + tid;
+        uint32_t v = 0;
+        if (s < A.num_scenes) v = __ldcg(&S.scenes[s].G2) * __ldcg(&S.scenes[s].G3);
+        uint32_t x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        if (lane == 31) s_wsum[wid] = x;
+        __syncthreads();
+        uint32_t pre = 0;
+        for (uint32_t w = 0; w < wid; ++w) pre += s_wsum[w];
+        uint32_t excl = s_carry + pre + x - v;
+        if (s < A.num_scenes) S.scenes[s].bucket_base = excl;
+        __syncthreads();
+        if (tid == kThreads - 1) s_carry = excl + v;
+        __syncthreads();
+    }
+    Ctrl* C = S.ctrl;
+    if (tid == 0) {
+        uint32_t total = s_carry;
+        uint32_t bbits = 0;
+        while (bbits < 32 && (1ull << bbits) < (uint64_t)total) ++bbits;
+        uint32_t q = A.key_bits > bbits ? A.key_bits - bbits : 0u;
+        if (q > 24) q = 24;
+        if (q == 0) atomicOr(&C->error, kErrCellRange);
+        C->qbits = q;
+        C->key_bits = A.key_bits;
+        C->total_buckets = total;
+        C->entry_count = 0;
+        C->pair_count = 0ull;
+        for (int p = 0; p < kMaxPasses + 4; ++p) C->tile_ctr[p] = 0;
+        C->sweep_ctr = 0;
+        C->scan_ctr = 0;
+        C->scan_total = 0;
+        C->epoch = C->epoch + 1u;
+        C->scenes_done = 0;
+    }
+    for (int p = 0; p < kMaxPasses; ++p) C->hist[p][tid] = 0u;
+}
+
+cudaError_t launch_plan(const BpScratch& s, const BpArgs& a, cudaStream_t st) {
+    k_plan<<<1, 1024, 0, st>>>(s, a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pca(const BpScratch& s, const BpArgs& a, cudaStream_t st) {
+    k_pca<<<a.num_work, kThreads, 0, st>>>(s, a, s.entry_cap);
+    return cudaGetLastError();
+}
+
+}  // namespace gsap

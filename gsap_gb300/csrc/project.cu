@@ -1,0 +1,168 @@
+// K2: projection of every object onto the scene's axes, cell replication
+// and the radix histograms of the first sort.
+//
+// Replaces projectSubMultiple (sapDetection/SapKernel.cu:151-213, key =
+// u.c - r + quadrant * interval, id = i) and the 8x4 cell mask of
+// calBoxHashSub32 (SapKernel.cu:1506-1633) together with the four-quadrant
+// split about the origin and its cross pass (SapKernel.cu:557-635, :968-1059):
+// the generalisation is a 2-D grid of cells on the two secondary axes, each
+// cell a separate sweep segment.  An object gets one sweep entry per cell its
+// projected (u2, u3) box touches; the entry key is
+//   ((bucket_base(scene) + c2 * G3 + c3) << Q) | q(lo1)
+// with q the clamped quantisation of the lower bound on u1.  All projections
+// use directed rounding (the interval always contains the exact projection
+// of the box), and the cell and q maps are monotone, so no overlapping pair
+// can be lost: the exact 3-D test later decides.
+#include "internal.cuh"
+
+namespace gsap {
+
+// u.x over the box spanned by corners a, b (any order), rounded outward.
+__device__ __forceinline__ void project_box(const float* u, float3 a, float3 b, float& lo, float& hi) {
+    float l0 = fminf(__fmul_rd(u[0], a.x), __fmul_rd(u[0], b.x));
+    float l1 = fminf(__fmul_rd(u[1], a.y), __fmul_rd(u[1], b.y));
+    float l2 = fminf(__fmul_rd(u[2], a.z), __fmul_rd(u[2], b.z));
+    float h0 = fmaxf(__fmul_ru(u[0], a.x), __fmul_ru(u[0], b.x));
+    float h1 = fmaxf(__fmul_ru(u[1], a.y), __fmul_ru(u[1], b.y));
+    float h2 = fmaxf(__fmul_ru(u[2], a.z), __fmul_ru(u[2], b.z));
+    lo = __fadd_rd(__fadd_rd(l0, l1), l2);
+    hi = __fadd_ru(__fadd_ru(h0, h1), h2);
+}
+
+// Clamped monotone cell index.
+__device__ __forceinline__ uint32_t cell_of(float x, float org, float inv, uint32_t G) {
+    float t = __fmul_rn(__fsub_rn(x, org), inv);
+    t = fminf(fmaxf(t, 0.f), (float)(G - 1u));
+    return (uint32_t)t;
+}
+
+// Box corners of object i (sphere: centre -/+ |r|, rounded outward).
+__device__ __forceinline__ bool load_box(const BpArgs& A, uint32_t i, float3& a, float3& b) {
+    float4 p = A.mn[i];
+    if (A.mode == 0) {
+        float4 q = A.mx[i];
+        a = make_float3(p.x, p.y, p.z);
+        b = make_float3(q.x, q.y, q.z);
+    } else {
+        float r = fabsf(p.w);
+        a = make_float3(__fsub_rd(p.x, r), __fsub_rd(p.y, r), __fsub_rd(p.z, r));
+        b = make_float3(__fadd_ru(p.x, r), __fadd_ru(p.y, r), __fadd_ru(p.z, r));
+    }
+    return isfinite(a.x) && isfinite(a.y) && isfinite(a.z) && isfinite(b.x) && isfinite(b.y) && isfinite(b.z);
+}
+
+constexpr int kProjItems = kChunk / kThreads;  // 16 objects per thread
+
+template <int PASSES>
+__global__ void __launch_bounds__(kThreads) k_project(BpScratch S, BpArgs A) {
+    __shared__ uint32_t s_hist[PASSES][256];
+    __shared__ float s_f[16];
+    __shared__ uint32_t s_i[4];
+    __shared__ uint32_t s_wtot[kThreads / 32];
+    __shared__ uint32_t s_base;
+    const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    uint32_t scene, b, e, wfirst, nw;
+    if (!map_work(blockIdx.x, S, A, scene, b, e, wfirst, nw)) return;
+    for (uint32_t k = tid; k < PASSES * 256; k += kThreads) (&s_hist[0][0])[k] = 0u;
+    if (tid == 0) {
+        const Scene& sc = S.scenes[scene];
+        for (int k = 0; k < 9; ++k) s_f[k] = sc.u[k];
+        uint32_t Q = S.ctrl->qbits;
+        s_f[9] = sc.q_org;
+        s_f[10] = __fdiv_rn((float)(1u << Q), sc.q_range);
+        s_f[11] = sc.c2_org;
+        s_f[12] = sc.c2_inv;
+        s_f[13] = sc.c3_org;
+        s_f[14] = sc.c3_inv;
+        s_i[0] = sc.G2;
+        s_i[1] = sc.G3;
+        s_i[2] = sc.bucket_base;
+        s_i[3] = Q;
+    }
+    __syncthreads();
+    const uint32_t G2 = s_i[0], G3 = s_i[1], bb = s_i[2], Q = s_i[3];
+    const float qmax = (float)((1u << Q) - 1u);
+
+    uint32_t qlo[kProjItems], clo[kProjItems], ncl[kProjItems], pre[kProjItems];
+    uint32_t running = 0;
+    bool bad = false;
+    const uint32_t wb = b + wid * (32 * kProjItems);
+#pragma unroll
+    for (int k = 0; k < kProjItems; ++k) {
+        uint32_t i = wb + k * 32 + lane;
+        uint32_t r = 0;
+        qlo[k] = 0; clo[k] = 0; ncl[k] = 0;
+        if (i < e) {
+            float3 a, c;
+            if (load_box(A, i, a, c)) {
+                float l1, h1, l2, h2, l3, h3;
+                project_box(&s_f[0], a, c, l1, h1);
+                project_box(&s_f[3], a, c, l2, h2);
+                project_box(&s_f[6], a, c, l3, h3);
+                float t = __fmul_rn(__fsub_rn(l1, s_f[9]), s_f[10]);
+                qlo[k] = (uint32_t)fminf(fmaxf(t, 0.f), qmax);
+                uint32_t c2a = cell_of(l2, s_f[11], s_f[12], G2), c2b = cell_of(h2, s_f[11], s_f[12], G2);
+                uint32_t c3a = cell_of(l3, s_f[13], s_f[14], G3), c3b = cell_of(h3, s_f[13], s_f[14], G3);
+                uint32_t n2 = c2b >= c2a ? c2b - c2a + 1 : 0, n3 = c3b >= c3a ? c3b - c3a + 1 : 0;
+                clo[k] = (c2a << 16) | c3a;
+                ncl[k] = (n2 << 16) | n3;
+                r = n2 * n3;
+                S.objcell[i] = clo[k];
+                if (S.objscene) S.objscene[i] = scene;
+            } else {
+                bad = true;
+            }
+        }
+        uint32_t x = r;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        pre[k] = running + x - r;
+        running += __shfl_sync(0xffffffffu, x, 31);
+    }
+    if (bad) atomicOr(&S.ctrl->error, kErrNonFinite);
+    if (lane == 0) s_wtot[wid] = running;
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t t = 0;
+        for (int w = 0; w < kThreads / 32; ++w) { uint32_t v = s_wtot[w]; s_wtot[w] = t; t += v; }
+        uint32_t base = atomicAdd(&S.ctrl->entry_count, t);
+        if ((uint64_t)base + t > S.entry_cap) atomicOr(&S.ctrl->error, kErrEntryCap);
+        s_base = base;
+    }
+    __syncthreads();
+    const uint64_t wpos = (uint64_t)s_base + s_wtot[wid];
+#pragma unroll
+    for (int k = 0; k < kProjItems; ++k) {
+        uint32_t n2 = ncl[k] >> 16, n3 = ncl[k] & 0xFFFFu;
+        if (n2 * n3 == 0) continue;
+        uint32_t i = wb + k * 32 + lane;
+        uint32_t c2a = clo[k] >> 16, c3a = clo[k] & 0xFFFFu;
+        uint64_t pos = wpos + pre[k];
+        for (uint32_t x2 = 0; x2 < n2; ++x2)
+            for (uint32_t x3 = 0; x3 < n3; ++x3, ++pos) {
+                uint32_t key = ((bb + (c2a + x2) * G3 + (c3a + x3)) << Q) | qlo[k];
+                if (pos < S.entry_cap) {  // entries past the capacity are counted, never stored
+                    S.keys[0][pos] = key;
+                    S.vals[0][pos] = i;
+#pragma unroll
+                    for (int p = 0; p < PASSES; ++p) atomicAdd(&s_hist[p][(key >> (8 * p)) & 255u], 1u);
+                }
+            }
+    }
+    __syncthreads();
+    for (uint32_t k = tid; k < PASSES * 256; k += kThreads) {
+        uint32_t v = (&s_hist[0][0])[k];
+        if (v) atomicAdd(&S.ctrl->hist[0][0] + k, v);
+    }
+}
+
+cudaError_t launch_project(const BpScratch& s, const BpArgs& a, int passes, cudaStream_t st) {
+    if (passes == 3) k_project<3><<<a.num_work, kThreads, 0, st>>>(s, a);
+    else k_project<4><<<a.num_work, kThreads, 0, st>>>(s, a);
+    return cudaGetLastError();
+}
+
+}  // namespace gsap

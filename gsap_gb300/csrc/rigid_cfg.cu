@@ -1,0 +1,226 @@
+// Particle rigid-body step, config model (FP32 state).
+//
+// The contact model of the 65,536-cube and batched scenes: linear spring k
+// on the penetration, normal damping eta, tangential damping kt * eta, six
+// walls of an axis-aligned box, gravity along y.  For a particle i and a
+// contact partner j (a particle, or a wall seen as a fixed particle):
+//   n = (p_j - p_i) / |p_j - p_i|,  pen = r_i + r_j - |p_j - p_i|,
+//   v = v_j - v_i,  f_i += -k pen n + eta (v.n) n + kt eta (v - (v.n) n).
+// The step order is the reference's (cudaPhysics/demoParticles.h:875-912):
+// integrate, place particles, broadphase, forces, velocity update; the
+// velocity update uses I_w^-1 = R I_shape^-1 R^T (prepareK,
+// ParticleRigidBodyKernel.h:30-45) rather than the reference's
+// angVel += tau dt (:260-261).
+//
+// Kernels: one thread per particle for placement and forces (each particle
+// gathers from the particles of the bodies that overlap its own body, in
+// neighbour-id order, and writes its force once, no read-modify-write); one
+// thread per body for the body AABB and for the compensated (two-sum)
+// per-body force / torque reduction fused with the velocity update.
+#include "internal.cuh"
+#include "rigid.cuh"
+
+namespace gsap {
+
+__device__ __forceinline__ void qrows(float4 q, float3 r[3]) {
+    float x = q.x, y = q.y, z = q.z, w = q.w;
+    r[0] = make_float3(1.f - 2.f * (y * y + z * z), 2.f * (x * y - w * z), 2.f * (x * z + w * y));
+    r[1] = make_float3(2.f * (x * y + w * z), 1.f - 2.f * (x * x + z * z), 2.f * (y * z - w * x));
+    r[2] = make_float3(2.f * (x * z - w * y), 2.f * (y * z + w * x), 1.f - 2.f * (x * x + y * y));
+}
+__device__ __forceinline__ float3 mv(const float3 r[3], float3 v) {
+    return make_float3(r[0].x * v.x + r[0].y * v.y + r[0].z * v.z, r[1].x * v.x + r[1].y * v.y + r[1].z * v.z,
+                       r[2].x * v.x + r[2].y * v.y + r[2].z * v.z);
+}
+__device__ __forceinline__ float3 cross3(float3 a, float3 b) {
+    return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+
+__global__ void k_integrate_cfg(float4* pos, float4* quat, float4* lin, const float4* ang, CfgParams p, int n) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    float4 v = lin[b];
+    v.y += p.gy * p.dt;
+    lin[b] = v;
+    float4 q = quat[b], w = ang[b];
+    // (w, 0) (x) q = (q.w w + w x q_v, -w . q_v)
+    float dx = q.w * w.x + (w.y * q.z - w.z * q.y);
+    float dy = q.w * w.y + (w.z * q.x - w.x * q.z);
+    float dz = q.w * w.z + (w.x * q.y - w.y * q.x);
+    float dw = -(w.x * q.x + w.y * q.y + w.z * q.z);
+    float h = 0.5f * p.dt;
+    q.x += h * dx; q.y += h * dy; q.z += h * dz; q.w += h * dw;
+    float il = rsqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
+    q.x *= il; q.y *= il; q.z *= il; q.w *= il;
+    quat[b] = q;
+    float4 x = pos[b];
+    x.x += v.x * p.dt; x.y += v.y * p.dt; x.z += v.z * p.dt;
+    pos[b] = x;
+}
+
+__global__ void k_place_cfg(const float4* pos, const float4* quat, const float4* lin, const float4* ang,
+                            const int* shape, const int* pstart, const int* p_body, const float4* ref_pos,
+                            float4* p_pos, float4* p_vel, int np) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    int b = p_body[i];
+    float4 ref = ref_pos[kMaxParticlesPerBody * shape[b] + (i - pstart[b])];
+    float3 R[3];
+    qrows(quat[b], R);
+    float3 r = mv(R, make_float3(ref.x, ref.y, ref.z));
+    float4 x = pos[b], v = lin[b], w = ang[b];
+    float3 wr = cross3(make_float3(w.x, w.y, w.z), r);
+    p_pos[i] = make_float4(x.x + r.x, x.y + r.y, x.z + r.z, ref.w);
+    p_vel[i] = make_float4(v.x + wr.x, v.y + wr.y, v.z + wr.z, 0.f);
+}
+
+__global__ void k_body_aabb(const float4* p_pos, const int* pstart, const int* npart, float4* bmin, float4* bmax,
+                            int n) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    int s = pstart[b], m = npart[b];
+    float3 lo = make_float3(INFINITY, INFINITY, INFINITY), hi = make_float3(-INFINITY, -INFINITY, -INFINITY);
+    for (int k = 0; k < m; ++k) {
+        float4 p = p_pos[s + k];
+        float r = fabsf(p.w);
+        lo.x = fminf(lo.x, __fsub_rd(p.x, r)); lo.y = fminf(lo.y, __fsub_rd(p.y, r)); lo.z = fminf(lo.z, __fsub_rd(p.z, r));
+        hi.x = fmaxf(hi.x, __fadd_ru(p.x, r)); hi.y = fmaxf(hi.y, __fadd_ru(p.y, r)); hi.z = fmaxf(hi.z, __fadd_ru(p.z, r));
+    }
+    if (m == 0) { lo = make_float3(0.f, 0.f, 0.f); hi = make_float3(-1.f, -1.f, -1.f); }
+    bmin[b] = make_float4(lo.x, lo.y, lo.z, 0.f);
+    bmax[b] = make_float4(hi.x, hi.y, hi.z, 0.f);
+}
+
+__device__ __forceinline__ void contact(const CfgParams& p, float3 n, float pen, float3 v, float3& f) {
+    float vn = v.x * n.x + v.y * n.y + v.z * n.z;
+    float ks = -p.k * pen + p.eta * vn;
+    float kt = p.kt * p.eta;
+    f.x += ks * n.x + kt * (v.x - vn * n.x);
+    f.y += ks * n.y + kt * (v.y - vn * n.y);
+    f.z += ks * n.z + kt * (v.z - vn * n.z);
+}
+
+__global__ void __launch_bounds__(256) k_forces_cfg(const float4* __restrict__ p_pos, const float4* __restrict__ p_vel,
+                                                    const int* p_body, const int* pstart, const int* npart,
+                                                    const uint2* body_pairs, const uint32_t* rowoff, CfgParams p,
+                                                    float4* p_force, int np) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    float4 ip = p_pos[i], iv = p_vel[i];
+    float3 f = make_float3(0.f, 0.f, 0.f);
+    float3 vw = make_float3(-iv.x, -iv.y, -iv.z);
+    const float pc[3] = {ip.x, ip.y, ip.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float pen_lo = ip.w - (pc[a] - p.lo[a]);
+        float pen_hi = ip.w - (p.hi[a] - pc[a]);
+        if (pen_lo > 0.f) {
+            float3 n = make_float3(a == 0 ? -1.f : 0.f, a == 1 ? -1.f : 0.f, a == 2 ? -1.f : 0.f);
+            contact(p, n, pen_lo, vw, f);
+        }
+        if (pen_hi > 0.f) {
+            float3 n = make_float3(a == 0 ? 1.f : 0.f, a == 1 ? 1.f : 0.f, a == 2 ? 1.f : 0.f);
+            contact(p, n, pen_hi, vw, f);
+        }
+    }
+    int a = p_body[i];
+    uint32_t e0 = rowoff[a], e1 = rowoff[a + 1];
+    for (uint32_t e = e0; e < e1; ++e) {
+        int b = (int)__ldg(&body_pairs[e].y);
+        int s = __ldg(pstart + b), m = __ldg(npart + b);
+        for (int l = 0; l < m; ++l) {
+            float4 jp = __ldg(p_pos + s + l);
+            float dx = jp.x - ip.x, dy = jp.y - ip.y, dz = jp.z - ip.z;
+            float d2 = dx * dx + dy * dy + dz * dz;
+            float rr = ip.w + jp.w;
+            if (d2 < rr * rr && d2 > 0.f) {
+                float dist = sqrtf(d2);
+                float inv = 1.f / dist;
+                float4 jv = __ldg(p_vel + s + l);
+                float3 n = make_float3(dx * inv, dy * inv, dz * inv);
+                contact(p, n, rr - dist, make_float3(jv.x - iv.x, jv.y - iv.y, jv.z - iv.z), f);
+            }
+        }
+    }
+    p_force[i] = make_float4(f.x, f.y, f.z, 0.f);
+}
+
+__device__ __forceinline__ void ts_add(float& s, float& c, float x) {
+    float t = s + x;
+    float bp = t - s;
+    c += (s - (t - bp)) + (x - bp);
+    s = t;
+}
+
+__global__ void k_update_cfg(float4* lin, float4* ang, const float4* quat, const float* inv_mass, const int* shape,
+                             const int* pstart, const int* npart, const float4* ref_pos, const float4* shape_inv,
+                             const float4* p_force, CfgParams p, int n) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n) return;
+    float3 R[3];
+    qrows(quat[b], R);
+    int s = pstart[b], m = npart[b], sh = shape[b];
+    float F[3] = {0, 0, 0}, Fc[3] = {0, 0, 0}, T[3] = {0, 0, 0}, Tc[3] = {0, 0, 0};
+    for (int k = 0; k < m; ++k) {
+        float4 ref = ref_pos[kMaxParticlesPerBody * sh + k];
+        float3 r = mv(R, make_float3(ref.x, ref.y, ref.z));
+        float4 f4 = p_force[s + k];
+        float3 f = make_float3(f4.x, f4.y, f4.z);
+        float3 t = cross3(r, f);
+        ts_add(F[0], Fc[0], f.x); ts_add(F[1], Fc[1], f.y); ts_add(F[2], Fc[2], f.z);
+        ts_add(T[0], Tc[0], t.x); ts_add(T[1], Tc[1], t.y); ts_add(T[2], Tc[2], t.z);
+    }
+    float3 Fs = make_float3(F[0] + Fc[0], F[1] + Fc[1], F[2] + Fc[2]);
+    float3 Ts = make_float3(T[0] + Tc[0], T[1] + Tc[1], T[2] + Tc[2]);
+    float im = inv_mass[b];
+    float4 v = lin[b];
+    v.x += Fs.x * im * p.dt; v.y += Fs.y * im * p.dt; v.z += Fs.z * im * p.dt;
+    lin[b] = v;
+    // I_w^-1 tau = R (I_s^-1 (R^T tau))
+    float3 t1 = make_float3(R[0].x * Ts.x + R[1].x * Ts.y + R[2].x * Ts.z,
+                            R[0].y * Ts.x + R[1].y * Ts.y + R[2].y * Ts.z,
+                            R[0].z * Ts.x + R[1].z * Ts.y + R[2].z * Ts.z);
+    float4 i0 = shape_inv[3 * sh], i1 = shape_inv[3 * sh + 1], i2 = shape_inv[3 * sh + 2];
+    float3 t2 = make_float3(i0.x * t1.x + i0.y * t1.y + i0.z * t1.z, i1.x * t1.x + i1.y * t1.y + i1.z * t1.z,
+                            i2.x * t1.x + i2.y * t1.y + i2.z * t1.z);
+    float3 dw = mv(R, t2);
+    float4 w = ang[b];
+    w.x += dw.x * p.dt; w.y += dw.y * p.dt; w.z += dw.z * p.dt;
+    ang[b] = w;
+}
+
+static inline int gr(int n) { return n <= 0 ? 1 : (n + 255) / 256; }
+
+cudaError_t rb_integrate_cfg(float4* pos, float4* quat, float4* lin, const float4* ang, const CfgParams& p, int n,
+                             cudaStream_t st) {
+    if (n > 0) k_integrate_cfg<<<gr(n), 256, 0, st>>>(pos, quat, lin, ang, p, n);
+    return cudaGetLastError();
+}
+cudaError_t rb_place_cfg(const float4* pos, const float4* quat, const float4* lin, const float4* ang,
+                         const int* shape, const int* pstart, const int* p_body, const float4* ref_pos,
+                         float4* p_pos, float4* p_vel, int np, cudaStream_t st) {
+    if (np > 0) k_place_cfg<<<gr(np), 256, 0, st>>>(pos, quat, lin, ang, shape, pstart, p_body, ref_pos, p_pos, p_vel, np);
+    return cudaGetLastError();
+}
+cudaError_t rb_body_aabb(const float4* p_pos, const int* pstart, const int* npart, float4* bmin, float4* bmax, int n,
+                         cudaStream_t st) {
+    if (n > 0) k_body_aabb<<<gr(n), 256, 0, st>>>(p_pos, pstart, npart, bmin, bmax, n);
+    return cudaGetLastError();
+}
+cudaError_t rb_forces_cfg(const float4* p_pos, const float4* p_vel, const int* p_body, const int* pstart,
+                          const int* npart, const uint2* body_pairs, const uint32_t* rowoff, const CfgParams& p,
+                          float4* p_force, int np, cudaStream_t st) {
+    if (np > 0)
+        k_forces_cfg<<<gr(np), 256, 0, st>>>(p_pos, p_vel, p_body, pstart, npart, body_pairs, rowoff, p, p_force, np);
+    return cudaGetLastError();
+}
+cudaError_t rb_update_cfg(float4* lin, float4* ang, const float4* quat, const float* inv_mass, const int* shape,
+                          const int* pstart, const int* npart, const float4* ref_pos, const float4* shape_inv,
+                          const float4* p_force, const CfgParams& p, int n, cudaStream_t st) {
+    if (n > 0)
+        k_update_cfg<<<gr(n), 256, 0, st>>>(lin, ang, quat, inv_mass, shape, pstart, npart, ref_pos, shape_inv, p_force,
+                                            p, n);
+    return cudaGetLastError();
+}
+
+}  // namespace gsap

@@ -1,0 +1,200 @@
+// K3: onesweep LSD radix sort of (u32 key, u32 value) with 8-bit digits.
+//
+// Replaces the NVIDIA SDK radix sort of the reference
+// (sapDetection/radixsort.cu:1116-1348 radixSortStep: per pass a 1024-key
+// CTA-local split sort, findRadixOffsets, a CUDPP scan of the counters and
+// reorderData, i.e. four launches and a library scan per 4-bit digit).
+// Here every pass is one launch: the digit histograms of all passes were
+// counted up front (fused into the projection kernel), each CTA ranks a
+// 4096-key tile with warp ballots (eight ballots give every lane the mask of
+// lanes holding the same digit), publishes its per-digit counts, and finds
+// its global offsets by a decoupled look-back over earlier tiles.  Tiles are
+// handed out in order by an atomic counter, so a tile only ever waits on
+// tiles that running CTAs own; every wait is bounded and reports
+// GSAP_ERR_DEVICE_TIMEOUT instead of hanging.  Stable: equal digits keep
+// their input order, so the passes give the order of a stable sort.
+#include "internal.cuh"
+
+namespace gsap {
+
+// Exclusive scan over the 256 threads of a CTA; returns the exclusive value.
+__device__ __forceinline__ uint32_t cta_excl_scan256(uint32_t v, uint32_t* s_w) {
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) s_w[wid] = x;
+    __syncthreads();
+    uint32_t pre = 0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w)
+        if ((uint32_t)w < wid) pre += s_w[w];
+    __syncthreads();
+    return pre + x - v;
+}
+
+template <int ITEMS>
+__global__ void __launch_bounds__(kThreads) k_onesweep(BpScratch S, const uint32_t* __restrict__ kin,
+                                                       const uint32_t* __restrict__ vin,
+                                                       uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
+                                                       const uint32_t* count_ptr, uint32_t cap, int pass,
+                                                       uint32_t spin) {
+    constexpr int TILE = kThreads * ITEMS;
+    __shared__ uint32_t s_k[TILE];
+    __shared__ uint32_t s_v[TILE];
+    __shared__ uint32_t s_wh[kThreads / 32][256];
+    __shared__ uint32_t s_gdig[256];
+    __shared__ uint32_t s_start[256];
+    __shared__ uint32_t s_gb[256];
+    __shared__ uint32_t s_scan[8];
+    __shared__ uint32_t s_tile;
+    const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const uint32_t n = min(*count_ptr, cap);
+    const uint32_t ntiles = (n + TILE - 1) / TILE;
+    const int shift = 8 * pass;
+    const uint32_t tag = (S.ctrl->epoch << 3) | (uint32_t)pass;
+    const uint32_t lt = lanemask_lt();
+
+    s_gdig[tid] = cta_excl_scan256(S.ctrl->hist[pass][tid], s_scan);
+
+    while (true) {
+        if (tid == 0) s_tile = atomicAdd(&S.ctrl->tile_ctr[pass], 1u);
+#pragma unroll
+        for (int w = 0; w < kThreads / 32; ++w) s_wh[w][tid] = 0u;
+        __syncthreads();
+        const uint32_t t = s_tile;
+        if (t >= ntiles) break;
+        const uint32_t tbase = t * TILE;
+        const uint32_t wb = tbase + wid * 32 * ITEMS;
+        uint32_t key[ITEMS], val[ITEMS], rk[ITEMS];
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            uint32_t idx = wb + k * 32 + lane;
+            if (idx < n) {
+                key[k] = __ldcs(kin + idx);
+                val[k] = __ldcs(vin + idx);
+            } else {
+                key[k] = 0u;
+                val[k] = 0u;
+            }
+        }
+        // warp-level multi-split ranking, items in index order
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            const bool valid = wb + k * 32 + lane < n;
+            const uint32_t d = (key[k] >> shift) & 255u;
+            uint32_t m = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+            for (int bit = 0; bit < 8; ++bit) {
+                uint32_t bal = __ballot_sync(0xffffffffu, (d >> bit) & 1u);
+                m &= ((d >> bit) & 1u) ? bal : ~bal;
+            }
+            uint32_t before = valid ? s_wh[wid][d] : 0u;
+            uint32_t r = __popc(m & lt);
+            __syncwarp();
+            if (valid && r == 0) s_wh[wid][d] = before + __popc(m);
+            __syncwarp();
+            rk[k] = before + r;
+        }
+        __syncthreads();
+        // per digit: exclusive warp offsets and the tile count
+        uint32_t tot = 0;
+#pragma unroll
+        for (int w = 0; w < kThreads / 32; ++w) {
+            uint32_t c = s_wh[w][tid];
+            s_wh[w][tid] = tot;
+            tot += c;
+        }
+        uint64_t* st = S.status + (uint64_t)t * 256u + tid;
+        st_release_u64(st, lb_word(tag, t == 0 ? kFlagPrefix : kFlagAgg, tot));
+        s_start[tid] = cta_excl_scan256(tot, s_scan);
+        uint32_t excl = 0;
+        if (t > 0) {
+            excl = lookback(S.status, t, tid, 256u, tag, spin, &S.ctrl->error);
+            st_release_u64(st, lb_word(tag, kFlagPrefix, excl + tot));
+        }
+        s_gb[tid] = s_gdig[tid] + excl - s_start[tid];
+        __syncthreads();
+        // stage the tile in digit order
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            if (wb + k * 32 + lane < n) {
+                uint32_t d = (key[k] >> shift) & 255u;
+                uint32_t lp = s_start[d] + s_wh[wid][d] + rk[k];
+                s_k[lp] = key[k];
+                s_v[lp] = val[k];
+            }
+        }
+        __syncthreads();
+        const uint32_t tn = min((uint32_t)TILE, n - tbase);
+        for (uint32_t i = tid; i < tn; i += kThreads) {
+            uint32_t kk = s_k[i];
+            uint32_t g = s_gb[(kk >> shift) & 255u] + i;
+            kout[g] = kk;
+            vout[g] = s_v[i];
+        }
+        __syncthreads();
+    }
+}
+
+// Histograms of all passes for a standalone sort.
+template <int PASSES>
+__global__ void __launch_bounds__(kThreads) k_hist(Ctrl* C, const uint32_t* __restrict__ keys, uint32_t n) {
+    __shared__ uint32_t s_hist[PASSES][256];
+    for (uint32_t k = threadIdx.x; k < PASSES * 256; k += kThreads) (&s_hist[0][0])[k] = 0u;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+        uint32_t key = keys[i];
+#pragma unroll
+        for (int p = 0; p < PASSES; ++p) atomicAdd(&s_hist[p][(key >> (8 * p)) & 255u], 1u);
+    }
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < PASSES * 256; k += kThreads) {
+        uint32_t v = (&s_hist[0][0])[k];
+        if (v) atomicAdd(&C->hist[0][0] + k, v);
+    }
+}
+
+// Counter reset + new epoch for a standalone sort.
+__global__ void k_sort_reset(Ctrl* C, uint32_t n, uint32_t* count_slot) {
+    uint32_t t = threadIdx.x;
+    for (int p = 0; p < kMaxPasses; ++p) C->hist[p][t] = 0u;
+    if (t == 0) {
+        for (int p = 0; p < kMaxPasses + 4; ++p) C->tile_ctr[p] = 0;
+        C->epoch = C->epoch + 1u;
+        *count_slot = n;
+    }
+}
+
+cudaError_t launch_sort_prep(const BpScratch& s, const uint32_t* keys, const uint32_t* count_ptr, uint32_t n,
+                             int passes, cudaStream_t st) {
+    k_sort_reset<<<1, 256, 0, st>>>(s.ctrl, n, const_cast<uint32_t*>(count_ptr));
+    int grid = sm_count() * 4;
+    switch (passes) {
+        case 1: k_hist<1><<<grid, kThreads, 0, st>>>(s.ctrl, keys, n); break;
+        case 2: k_hist<2><<<grid, kThreads, 0, st>>>(s.ctrl, keys, n); break;
+        case 3: k_hist<3><<<grid, kThreads, 0, st>>>(s.ctrl, keys, n); break;
+        default: k_hist<4><<<grid, kThreads, 0, st>>>(s.ctrl, keys, n); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sort_pass(const BpScratch& s, int pass, int passes, const uint32_t* kin, const uint32_t* vin,
+                             uint32_t* kout, uint32_t* vout, const uint32_t* count_ptr, uint64_t cap,
+                             uint32_t spin, cudaStream_t st) {
+    (void)passes;
+    static int grid = 0;
+    if (grid == 0) {
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_onesweep<kSortItems>, kThreads, 0);
+        grid = sm_count() * (per_sm > 0 ? per_sm : 1);
+    }
+    uint32_t c = cap > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)cap;
+    k_onesweep<kSortItems><<<grid, kThreads, 0, st>>>(s, kin, vin, kout, vout, count_ptr, c, pass, spin);
+    return cudaGetLastError();
+}
+
+}  // namespace gsap

@@ -1,0 +1,162 @@
+// K4: the sweep.
+//
+// Replaces the reference's sweep set-up and candidate kernels
+// (sapDetection/SapKernel.cu:2448-2517: reorderSphere, calBoxHashSub32,
+// CounterThreadSphPCATexSub + CUDPP scan + a blocking read of the thread
+// total, assignThreadIDSphere, ZeroSetSphere, kernel_SphereTexCullPCAElong
+// :1810-1921 writing a column-major candidate matrix, a second CUDPP scan, a
+// second blocking read and the compaction assemPairsSphereSub :1649-1695),
+// and the cross pass of SapKernel.cu:2364-2446.
+//
+// Persistent warps take 32 consecutive sorted entries at a time from an
+// atomic counter (work stealing).  Each lane scans forward from its entry
+// while the candidate key is <= (bucket | q(hi1)): the q map is monotone, so
+// every later entry of the same cell whose interval on u1 can meet this one
+// is visited, and the scan stops at the cell (and scene) boundary by
+// construction.  Candidates pass the exact test on the original FP32 bounds
+// (closed AABB test of Aabb::overlaps, include/aabb.h:47-57, or the strict
+// squared sphere test of SapKernel.cu:1897-1903 with one rounding per
+// operation) and the owner-cell rule: a pair is reported only in the cell
+// holding max(lo2_i, lo2_j), max(lo3_i, lo3_j), which both objects touch, so
+// each overlapping pair comes out exactly once and no sort + unique pass is
+// needed.  Hits are compacted through a per-warp shared-memory buffer that
+// reserves global space with one atomic per 128 pairs.
+#include "internal.cuh"
+
+namespace gsap {
+
+__device__ __forceinline__ float proj_hi(const float* u, float3 a, float3 b) {
+    float h0 = fmaxf(__fmul_ru(u[0], a.x), __fmul_ru(u[0], b.x));
+    float h1 = fmaxf(__fmul_ru(u[1], a.y), __fmul_ru(u[1], b.y));
+    float h2 = fmaxf(__fmul_ru(u[2], a.z), __fmul_ru(u[2], b.z));
+    return __fadd_ru(__fadd_ru(h0, h1), h2);
+}
+
+constexpr int kBuf = 128;
+
+template <int MODE>
+__global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const uint32_t* __restrict__ keys,
+                                                    const uint32_t* __restrict__ vals, uint2* __restrict__ pairs,
+                                                    uint64_t pair_cap, int count_rows) {
+    __shared__ uint2 s_buf[kThreads / 32][kBuf];
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t lt = lanemask_lt();
+    Ctrl* C = S.ctrl;
+    const uint32_t E = (uint32_t)min((uint64_t)C->entry_count, S.entry_cap);
+    const uint32_t Q = C->qbits;
+    const uint32_t qmask = (1u << Q) - 1u;
+    const float qmax = (float)qmask;
+    uint32_t nbuf = 0;
+
+    auto flush = [&]() {
+        __syncwarp();
+        unsigned long long base = 0;
+        if (lane == 0 && nbuf) base = atomicAdd(&C->pair_count, (unsigned long long)nbuf);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        for (uint32_t k = lane; k < nbuf; k += 32) {
+            uint2 p = s_buf[wid][k];
+            if (base + k < pair_cap) {  // rows count stored pairs only: the scatter undoes exactly these
+                pairs[base + k] = p;
+                if (count_rows) {
+                    atomicAdd(&S.rowcnt[p.x], 1u);
+                    if (count_rows == 2) atomicAdd(&S.rowcnt[p.y], 1u);
+                }
+            }
+        }
+        __syncwarp();
+        nbuf = 0;
+    };
+
+    while (true) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&C->sweep_ctr, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= E) break;
+        const uint32_t e = base + lane;
+        bool live = e < E;
+        uint32_t i = 0, kb = 0, c2 = 0, c3 = 0, ci = 0;
+        float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), pb = pa;
+        if (live) {
+            const uint32_t key = keys[e];
+            i = vals[e];
+            const uint32_t s = S.objscene ? S.objscene[i] : 0u;
+            const Scene* sc = &S.scenes[s];
+            pa = A.mn[i];
+            float3 a, b;
+            if (MODE == 0) {
+                pb = A.mx[i];
+                a = make_float3(pa.x, pa.y, pa.z);
+                b = make_float3(pb.x, pb.y, pb.z);
+            } else {
+                float r = fabsf(pa.w);
+                a = make_float3(__fsub_rd(pa.x, r), __fsub_rd(pa.y, r), __fsub_rd(pa.z, r));
+                b = make_float3(__fadd_ru(pa.x, r), __fadd_ru(pa.y, r), __fadd_ru(pa.z, r));
+            }
+            float u[3] = {sc->u[0], sc->u[1], sc->u[2]};
+            float h1 = proj_hi(u, a, b);
+            float qs = __fdiv_rn((float)(1u << Q), sc->q_range);
+            float t = __fmul_rn(__fsub_rn(h1, sc->q_org), qs);
+            uint32_t qh = (uint32_t)fminf(fmaxf(t, 0.f), qmax);
+            kb = (key & ~qmask) | qh;
+            uint32_t local = (key >> Q) - sc->bucket_base;
+            uint32_t G3 = sc->G3;
+            c2 = local / G3;
+            c3 = local - c2 * G3;
+            ci = S.objcell[i];
+        }
+        uint32_t j = e + 1;
+        while (true) {
+            bool act = live && j < E;
+            if (act) act = __ldg(keys + j) <= kb;
+            live = act;
+            if (!__any_sync(0xffffffffu, act)) break;
+            bool hit = false;
+            uint32_t o = 0;
+            if (act) {
+                o = __ldg(vals + j);
+                float4 qa = __ldg(A.mn + o);
+                bool ov;
+                if (MODE == 0) {
+                    float4 qb = __ldg(A.mx + o);
+                    ov = pa.x <= qb.x && qa.x <= pb.x && pa.y <= qb.y && qa.y <= pb.y && pa.z <= qb.z &&
+                         qa.z <= pb.z;
+                } else {
+                    float dx = __fsub_rn(pa.x, qa.x), dy = __fsub_rn(pa.y, qa.y), dz = __fsub_rn(pa.z, qa.z);
+                    float t1 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                    float r = __fadd_rn(pa.w, qa.w);
+                    ov = t1 < __fmul_rn(r, r);
+                }
+                if (ov) {
+                    uint32_t co = __ldg(S.objcell + o);
+                    hit = max(ci >> 16, co >> 16) == c2 && max(ci & 0xFFFFu, co & 0xFFFFu) == c3;
+                }
+            }
+            uint32_t hm = __ballot_sync(0xffffffffu, hit);
+            if (hm) {
+                uint32_t cnt = __popc(hm);
+                if (nbuf + cnt > kBuf) flush();
+                if (hit) s_buf[wid][nbuf + __popc(hm & lt)] = make_uint2(min(i, o), max(i, o));
+                nbuf += cnt;
+            }
+            ++j;
+        }
+    }
+    flush();
+}
+
+cudaError_t launch_sweep(const BpScratch& s, const BpArgs& a, const uint32_t* keys, const uint32_t* vals,
+                         uint2* pairs, uint64_t pair_cap, int count_rows, cudaStream_t st) {
+    static int grid[2] = {0, 0};
+    int m = a.mode == 1 ? 1 : 0;
+    if (grid[m] == 0) {
+        int per_sm = 0;
+        if (m == 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep<0>, kThreads, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep<1>, kThreads, 0);
+        grid[m] = sm_count() * (per_sm > 0 ? per_sm : 1);
+    }
+    if (m == 0) k_sweep<0><<<grid[m], kThreads, 0, st>>>(s, a, keys, vals, pairs, pair_cap, count_rows);
+    else k_sweep<1><<<grid[m], kThreads, 0, st>>>(s, a, keys, vals, pairs, pair_cap, count_rows);
+    return cudaGetLastError();
+}
+
+}  // namespace gsap

@@ -1,0 +1,29 @@
+/*
+ * gsap_debug.h -- test hooks of libgsap.so that run on the host (no GPU).
+ * No counterpart in the reference: they expose internals of this
+ * implementation so that the CPU test suite can check them.
+ */
+#ifndef GSAP_DEBUG_H
+#define GSAP_DEBUG_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Host build of the FP64 per-scene solver that the PCA kernel runs in its
+ * last CTA: sums18 = (sum d[3], sum d d^T[6: xx xy xz yy yz zz], sum h[3],
+ * sum h h^T[6]) with d = centre - pilot, hmax3, pilot3, n objects of a scene
+ * in a call of n_total objects.  out17 = axes u1,u2,u3 (rows), eigenvalues,
+ * mean, G2, G3.  Returns 0 on success. */
+int gsap_debug_scene_solve(const double* sums18, const double* hmax3, const double* pilot3, double n,
+                           uint32_t n_total, uint32_t axis_mode, float cell_factor, uint32_t key_bits,
+                           uint64_t entry_cap, double* out17);
+
+/* Sizes of internal device structures (control block, scene record, PCA
+ * partial, sort tile) for layout checks.  Returns 0. */
+int gsap_debug_sizes(uint32_t* out4);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

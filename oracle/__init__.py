@@ -1,0 +1,229 @@
+"""CPU oracle for the gSap broadphase and particle rigid-body step.
+
+TEST INFRASTRUCTURE ONLY.  Imported by ``tests/``, ``__graft_entry__.smoke()``
+and the CPU legs of ``bench.py`` -- as the checker and the timed CPU baseline,
+never as the thing measured on the GPU.  The product package ``gsap_gb300``
+never imports it.
+
+``liboracle.so`` is the C restatement of the reference (``bp.c``, ``rb.c``;
+each routine cites the reference file:line it follows).  ``_ref/libgsapref.so``
+is built only where the reference tree is mounted: it compiles the
+reference's own ``Aabb::overlaps`` and particle rigid-body kernels for the
+host and is used to pin the restatement and to generate ``tests/golden``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+_REF = None
+
+
+_BUILT = False
+
+
+def build(ref: bool = False) -> None:
+    """Compile liboracle.so (always from source: a library built on another
+    machine type is never reused) and the reference harness when ``ref``."""
+    global _BUILT
+    if not _BUILT:
+        subprocess.run(["make", "-s", "-B", "-C", HERE, "liboracle.so"], check=True)
+        _BUILT = True
+    if ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+
+
+def _i64(x):
+    return C.c_int64(int(x))
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(HERE, "liboracle.so")
+        build()
+        L = C.CDLL(path)
+        P = C.c_void_p
+        L.orc_bf_aabb.argtypes = [P, P, C.c_uint32, P, C.c_int64, C.c_int]
+        L.orc_bf_aabb.restype = C.c_int64
+        L.orc_bf_sphere.argtypes = [P, C.c_uint32, P, C.c_int64, C.c_int]
+        L.orc_bf_sphere.restype = C.c_int64
+        L.orc_sap_ref.argtypes = [C.c_int, P, P, C.c_uint32, P, C.c_int64, C.c_int]
+        L.orc_sap_ref.restype = C.c_int64
+        L.orc_both_directions.argtypes = [P, C.c_int64, P, P]
+        L.orc_both_directions.restype = C.c_int64
+        L.orc_radix_sort_u32.argtypes = [P, P, C.c_uint32, C.c_int]
+        L.orc_radix_sort_u32.restype = None
+        L.orc_float_flip.argtypes = [C.c_float]
+        L.orc_float_flip.restype = C.c_uint32
+        L.orc_rb_step_ref.argtypes = [P, P, C.c_int64, C.c_int]
+        L.orc_rb_step_ref.restype = C.c_int64
+        L.orc_rb_step_cfg_f64.argtypes = [P, P, C.c_int]
+        L.orc_rb_step_cfg_f64.restype = C.c_int64
+        _LIB = L
+    return _LIB
+
+
+def ref_lib():
+    """The reference-source harness, or None where it was not built."""
+    global _REF
+    if _REF is None:
+        path = os.path.join(HERE, "_ref", "libgsapref.so")
+        if not os.path.exists(path):
+            return None
+        _REF = C.CDLL(path)
+        _REF.ref_bf_aabb.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int64]
+        _REF.ref_bf_aabb.restype = C.c_int64
+    return _REF
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def _f4(a):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if a.ndim == 2 and a.shape[1] == 3:
+        a = np.ascontiguousarray(np.concatenate([a, np.zeros((a.shape[0], 1), np.float32)], 1))
+    return a
+
+
+def _run_pairs(fn, *args, cap=None):
+    """Call a pair-producing routine twice if the first capacity is short."""
+    cap = 1 << 16 if cap is None else cap
+    while True:
+        out = np.empty((max(cap, 1), 2), np.uint32)
+        n = fn(*args, _ptr(out), _i64(cap))
+        if n <= cap:
+            return out[:n].copy()
+        cap = int(n)
+
+
+def bf_aabb(mn, mx, threads=0):
+    """Sorted (i<j) uint32 pairs of the O(n^2) closed AABB test."""
+    mn, mx = _f4(mn), _f4(mx)
+    L = lib()
+    return _run_pairs(lambda a, b, p, c: L.orc_bf_aabb(a, b, C.c_uint32(len(mn)), p, c, threads),
+                      _ptr(mn), _ptr(mx))
+
+
+def bf_sphere(spheres, threads=0):
+    """Sorted (i<j) uint32 pairs of the strict squared sphere test."""
+    s = _f4(spheres)
+    L = lib()
+    return _run_pairs(lambda a, p, c: L.orc_bf_sphere(a, C.c_uint32(len(s)), p, c, threads), _ptr(s))
+
+
+def sap_ref(mode, mn, mx=None, threads=0):
+    """The reference SaP algorithm restated on the CPU (mode 0 AABB, 1 sphere)."""
+    mn = _f4(mn)
+    mx = _f4(mx) if mx is not None else None
+    L = lib()
+    return _run_pairs(lambda a, b, p, c: L.orc_sap_ref(mode, a, b, C.c_uint32(len(mn)), p, c, threads),
+                      _ptr(mn), _ptr(mx))
+
+
+def both_directions(pairs):
+    """Reference output format: both-direction int2 list and pairEntries."""
+    pairs = np.ascontiguousarray(pairs, dtype=np.uint32)
+    npairs = len(pairs)
+    out = np.empty((max(2 * npairs, 1), 2), np.int32)
+    maxid = int(pairs.max()) + 1 if npairs else 1
+    ent = np.empty(maxid, np.int32)
+    ne = lib().orc_both_directions(_ptr(pairs), _i64(npairs), _ptr(out), _ptr(ent))
+    return out[: 2 * npairs].copy(), ent[:ne].copy()
+
+
+def radix_sort_u32(keys, vals, bits=32):
+    k = np.ascontiguousarray(keys, dtype=np.uint32).copy()
+    v = np.ascontiguousarray(vals, dtype=np.uint32).copy()
+    lib().orc_radix_sort_u32(_ptr(k), _ptr(v), C.c_uint32(len(k)), bits)
+    return k, v
+
+
+def float_flip(x):
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    u = x.view(np.uint32)
+    mask = np.where(u & 0x80000000, np.uint32(0xFFFFFFFF), np.uint32(0x80000000))
+    return u ^ mask
+
+
+def ref_bf_aabb(mn, mx):
+    """The reference's own Aabb::overlaps in the Demo::cpuBroadphase loop."""
+    R = ref_lib()
+    if R is None:
+        raise RuntimeError("reference harness not built (make -C oracle ref)")
+    mn, mx = _f4(mn), _f4(mx)
+    return _run_pairs(lambda a, b, p, c: R.ref_bf_aabb(a, b, C.c_uint32(len(mn)), p, c),
+                      _ptr(mn), _ptr(mx))
+
+
+# ----------------------------------------------------------------- rigid body
+
+class RbStateF32(C.Structure):
+    _fields_ = [("n_bodies", C.c_int), ("n_particles", C.c_int)] + [
+        (name, C.c_void_p) for name in (
+            "pos", "quat", "lin_vel", "ang_vel", "shape_idx", "p_start", "n_part", "inv_mass",
+            "inv_inertia", "p_pos", "p_vel", "p_force", "p_mass", "ref_pos", "ref_mass",
+            "shape_inv_inertia")]
+
+
+class RefParams(C.Structure):
+    _fields_ = [("dt", C.c_float), ("sp_multip", C.c_float), ("dp_multip", C.c_float),
+                ("max_lin_vel", C.c_float), ("gravity_y", C.c_float),
+                ("floor_clamp", C.c_int), ("torque_quirk", C.c_int), ("pair_loop_quirk", C.c_int)]
+
+
+class CfgParams(C.Structure):
+    _fields_ = [("dt", C.c_double), ("k", C.c_double), ("eta", C.c_double), ("kt", C.c_double),
+                ("gravity_y", C.c_double), ("box_lo", C.c_double * 3), ("box_hi", C.c_double * 3)]
+
+
+class RbStateF64(C.Structure):
+    _fields_ = [("n_bodies", C.c_int), ("n_particles", C.c_int)] + [
+        (name, C.c_void_p) for name in (
+            "pos", "quat", "lin_vel", "ang_vel", "shape_idx", "p_start", "n_part", "scene",
+            "inv_mass", "ref_pos", "shape_inv_inertia", "p_pos", "p_vel", "p_force")]
+
+
+def rb_step_ref(state: dict, dt, sp_multip, dp_multip, max_lin_vel=0.0, gravity_y=-5.0,
+                floor_clamp=True, torque_quirk=True, pair_loop_quirk=False, max_pairs=1 << 22, threads=0):
+    """One reference-order FP32 step on a dict of numpy arrays (updated in place).
+
+    Keys: pos, quat, lin_vel, ang_vel (nb,4) f32; shape_idx, p_start, n_part (nb,) i32;
+    inv_mass (nb,) f32; inv_inertia (nb,12) f32; ref_pos (10*ns,4); ref_mass (10*ns,);
+    shape_inv_inertia (ns,12); p_pos, p_vel, p_force (np,4); p_mass (np,).
+    Returns the number of both-direction pairs.
+    """
+    s = RbStateF32()
+    s.n_bodies = len(state["pos"])
+    s.n_particles = len(state["p_pos"])
+    for name, _ in RbStateF32._fields_[2:]:
+        setattr(s, name, state[name].ctypes.data)
+    p = RefParams(dt, sp_multip, dp_multip, max_lin_vel, gravity_y, int(floor_clamp), int(torque_quirk),
+                  int(pair_loop_quirk))
+    n = lib().orc_rb_step_ref(C.byref(s), C.byref(p), _i64(max_pairs), threads)
+    if n < 0:
+        raise RuntimeError("oracle pair capacity exceeded")
+    return n
+
+
+def rb_step_cfg_f64(state: dict, params: dict, threads=0):
+    """One config-mode FP64 step on a dict of float64/int32 arrays (in place)."""
+    s = RbStateF64()
+    s.n_bodies = len(state["pos"])
+    s.n_particles = len(state["p_pos"])
+    for name, _ in RbStateF64._fields_[2:]:
+        arr = state.get(name)
+        setattr(s, name, arr.ctypes.data if arr is not None else None)
+    p = CfgParams()
+    p.dt, p.k, p.eta, p.kt, p.gravity_y = (params[k] for k in ("dt", "k", "eta", "kt", "gravity_y"))
+    for a in range(3):
+        p.box_lo[a] = params["box_lo"][a]
+        p.box_hi[a] = params["box_hi"][a]
+    return lib().orc_rb_step_cfg_f64(C.byref(s), C.byref(p), threads)

@@ -1,0 +1,363 @@
+/*
+ * CPU oracle, broadphase half.  TEST INFRASTRUCTURE ONLY (see oracle.h): the
+ * checker for libgsap.so, never part of the product path.
+ *
+ * Compiled with -O2 -ffp-contract=off (and OpenMP when available): every
+ * float expression is evaluated in source order with one rounding per
+ * operation, which is how the GPU kernels evaluate the same predicates.
+ */
+#include "oracle.h"
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+static int nthreads(int t) {
+#ifdef _OPENMP
+    return t > 0 ? t : omp_get_max_threads();
+#else
+    (void)t;
+    return 1;
+#endif
+}
+
+/* Aabb::overlaps (include/aabb.h:47-57): closed on all six faces. */
+static inline int aabb_overlap(const float* ai, const float* xi,
+                               const float* aj, const float* xj) {
+    return ai[0] <= xj[0] && aj[0] <= xi[0] &&
+           ai[1] <= xj[1] && aj[1] <= xi[1] &&
+           ai[2] <= xj[2] && aj[2] <= xi[2];
+}
+
+/* Squared strict sphere test of kernel_SphereTexCullPCAElong
+ * (sapDetection/SapKernel.cu:1897-1903): x0 = ci - cj per axis,
+ * t1 = x0*x0 + y0*y0 + z0*z0 (left to right), e1 = (ri + rj)^2, t1 < e1. */
+static inline int sphere_overlap(const float* a, const float* b) {
+    float dx = a[0] - b[0];
+    float dy = a[1] - b[1];
+    float dz = a[2] - b[2];
+    float r = a[3] + b[3];
+    float t1 = dx * dx + dy * dy + dz * dz;
+    float e1 = r * r;
+    return t1 < e1;
+}
+
+typedef int (*pair_pred)(const float*, const float*, uint32_t, uint32_t);
+
+static int pred_aabb_ix(const float* mn, const float* mx, uint32_t i, uint32_t j) {
+    return aabb_overlap(mn + 4 * (size_t)i, mx + 4 * (size_t)i, mn + 4 * (size_t)j, mx + 4 * (size_t)j);
+}
+static int pred_sphere_ix(const float* s, const float* unused, uint32_t i, uint32_t j) {
+    (void)unused;
+    return sphere_overlap(s + 4 * (size_t)i, s + 4 * (size_t)j);
+}
+
+/* Row-major brute force: count per row, prefix, fill.  Two passes keep the
+ * output in (i, j) order without per-thread buffers. */
+static int64_t brute_force(const float* a, const float* b, uint32_t n,
+                           uint32_t* pairs, int64_t cap, int threads,
+                           int (*pred)(const float*, const float*, uint32_t, uint32_t)) {
+    if (n < 2) return 0;
+    int64_t* rowc = (int64_t*)calloc((size_t)n + 1, sizeof(int64_t));
+    int nt = nthreads(threads);
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nt)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+        int64_t c = 0;
+        for (uint32_t j = (uint32_t)i + 1; j < n; ++j) c += pred(a, b, (uint32_t)i, j);
+        rowc[i + 1] = c;
+    }
+    for (uint32_t i = 0; i < n; ++i) rowc[i + 1] += rowc[i];
+    int64_t total = rowc[n];
+    if (pairs) {
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nt)
+        for (int64_t i = 0; i < (int64_t)n; ++i) {
+            int64_t o = rowc[i];
+            if (o >= cap) continue;
+            for (uint32_t j = (uint32_t)i + 1; j < n && o < cap; ++j) {
+                if (pred(a, b, (uint32_t)i, j)) {
+                    pairs[2 * o] = (uint32_t)i;
+                    pairs[2 * o + 1] = j;
+                    ++o;
+                }
+            }
+        }
+    }
+    free(rowc);
+    return total;
+}
+
+int64_t orc_bf_aabb(const float* mn, const float* mx, uint32_t n,
+                    uint32_t* pairs, int64_t cap, int threads) {
+    return brute_force(mn, mx, n, pairs, cap, threads, pred_aabb_ix);
+}
+
+int64_t orc_bf_sphere(const float* spheres, uint32_t n,
+                      uint32_t* pairs, int64_t cap, int threads) {
+    return brute_force(spheres, NULL, n, pairs, cap, threads, pred_sphere_ix);
+}
+
+/* ------------------------------------------------------------ radix sort */
+
+uint32_t orc_float_flip(float f) {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    uint32_t mask = (u & 0x80000000u) ? 0xFFFFFFFFu : 0x80000000u;
+    return u ^ mask;
+}
+
+void orc_radix_sort_u32(uint32_t* keys, uint32_t* vals, uint32_t n, int bits) {
+    if (n < 2 || bits <= 0) return;
+    uint32_t* k2 = (uint32_t*)malloc((size_t)n * 4);
+    uint32_t* v2 = (uint32_t*)malloc((size_t)n * 4);
+    uint32_t *ks = keys, *vs = vals, *kd = k2, *vd = v2;
+    for (int shift = 0; shift < bits; shift += 8) {
+        size_t cnt[257];
+        memset(cnt, 0, sizeof(cnt));
+        uint32_t mask = (bits - shift >= 8) ? 0xFFu : ((1u << (bits - shift)) - 1u);
+        for (uint32_t i = 0; i < n; ++i) cnt[((ks[i] >> shift) & mask) + 1]++;
+        for (int d = 0; d < 256; ++d) cnt[d + 1] += cnt[d];
+        for (uint32_t i = 0; i < n; ++i) {
+            size_t p = cnt[(ks[i] >> shift) & mask]++;
+            kd[p] = ks[i];
+            if (vals) vd[p] = vs[i];
+        }
+        uint32_t* t = ks; ks = kd; kd = t;
+        t = vs; vs = vd; vd = t;
+    }
+    if (ks != keys) {
+        memcpy(keys, ks, (size_t)n * 4);
+        if (vals) memcpy(vals, vs, (size_t)n * 4);
+    }
+    free(k2);
+    free(v2);
+}
+
+/* LSD radix sort of u64 keys (pair keys (i << 32) | j). */
+static void radix_sort_u64(uint64_t* keys, size_t n, int bits) {
+    if (n < 2) return;
+    uint64_t* tmp = (uint64_t*)malloc(n * 8);
+    uint64_t *s = keys, *d = tmp;
+    for (int shift = 0; shift < bits; shift += 8) {
+        size_t cnt[257];
+        memset(cnt, 0, sizeof(cnt));
+        for (size_t i = 0; i < n; ++i) cnt[((s[i] >> shift) & 0xFF) + 1]++;
+        for (int q = 0; q < 256; ++q) cnt[q + 1] += cnt[q];
+        for (size_t i = 0; i < n; ++i) d[cnt[(s[i] >> shift) & 0xFF]++] = s[i];
+        uint64_t* t = s; s = d; d = t;
+    }
+    if (s != keys) memcpy(keys, s, n * 8);
+    free(tmp);
+}
+
+/* ------------------------------------------------------ reference SaP (CPU) */
+
+typedef struct pvec { uint64_t* p; size_t n, cap; } pvec;
+static void pv_push(pvec* v, uint64_t x) {
+    if (v->n == v->cap) {
+        v->cap = v->cap ? v->cap * 2 : 1024;
+        v->p = (uint64_t*)realloc(v->p, v->cap * 8);
+    }
+    v->p[v->n++] = x;
+}
+
+/* Sweep one group of objects (ids[0..m)) along axis `ax`: sort by the lower
+ * end of the projected interval (the flipped-float radix sort of
+ * radixsort.cu), then scan forward while lo_j <= hi_i
+ * (SapKernel.cu:1880-1913: break once d_pos[cur] > d_pos[i] + 2r). */
+static void sweep_group(int mode, const float* mn, const float* mx, int ax,
+                        uint32_t* ids, uint32_t m, pvec* out, int nt) {
+    if (m < 2) return;
+    uint32_t* keys = (uint32_t*)malloc((size_t)m * 4);
+    float* lo = (float*)malloc((size_t)m * 4);
+    float* hi = (float*)malloc((size_t)m * 4);
+    for (uint32_t k = 0; k < m; ++k) {
+        uint32_t i = ids[k];
+        float l, h;
+        if (mode == 0) {
+            l = mn[4 * (size_t)i + ax];
+            h = mx[4 * (size_t)i + ax];
+        } else {
+            float c = mn[4 * (size_t)i + ax], r = mn[4 * (size_t)i + 3];
+            l = c - r;
+            h = c + r;
+        }
+        keys[k] = orc_float_flip(l);
+        (void)h;
+    }
+    orc_radix_sort_u32(keys, ids, m, 32);
+    for (uint32_t k = 0; k < m; ++k) {
+        uint32_t i = ids[k];
+        if (mode == 0) {
+            lo[k] = mn[4 * (size_t)i + ax];
+            hi[k] = mx[4 * (size_t)i + ax];
+        } else {
+            float c = mn[4 * (size_t)i + ax], r = mn[4 * (size_t)i + 3];
+            lo[k] = c - r;
+            hi[k] = c + r;
+        }
+    }
+#pragma omp parallel num_threads(nt)
+    {
+        pvec local = {0, 0, 0};
+#pragma omp for schedule(dynamic, 256)
+        for (int64_t a = 0; a < (int64_t)m; ++a) {
+            uint32_t i = ids[a];
+            float h = hi[a];
+            for (uint32_t b = (uint32_t)a + 1; b < m && lo[b] <= h; ++b) {
+                uint32_t j = ids[b];
+                int hit = mode == 0 ? pred_aabb_ix(mn, mx, i, j) : pred_sphere_ix(mn, NULL, i, j);
+                if (hit) {
+                    uint32_t x = i < j ? i : j, y = i < j ? j : i;
+                    pv_push(&local, ((uint64_t)x << 32) | y);
+                }
+            }
+        }
+#pragma omp critical
+        {
+            for (size_t q = 0; q < local.n; ++q) pv_push(out, local.p[q]);
+        }
+        free(local.p);
+    }
+    free(keys);
+    free(lo);
+    free(hi);
+}
+
+int64_t orc_sap_ref(int mode, const float* mn, const float* mx, uint32_t n,
+                    uint32_t* pairs, int64_t cap, int threads) {
+    if (n < 2) return 0;
+    int nt = nthreads(threads);
+    /* centres: sphere xyz, or AABB midpoints */
+    double mean[3] = {0, 0, 0}, var[3] = {0, 0, 0};
+    float* cen = (float*)malloc((size_t)n * 12);
+    for (uint32_t i = 0; i < n; ++i)
+        for (int k = 0; k < 3; ++k) {
+            float c = mode == 0 ? 0.5f * (mn[4 * (size_t)i + k] + mx[4 * (size_t)i + k])
+                                : mn[4 * (size_t)i + k];
+            cen[3 * (size_t)i + k] = c;
+            mean[k] += c;
+        }
+    for (int k = 0; k < 3; ++k) mean[k] /= n;
+    for (uint32_t i = 0; i < n; ++i)
+        for (int k = 0; k < 3; ++k) {
+            double d = cen[3 * (size_t)i + k] - mean[k];
+            var[k] += d * d;
+        }
+    /* axisVecMultiple (SapKernel.cu:63-97): argmax of the covariance
+     * diagonal with the reference's tie order, secondary axes fixed. */
+    int axis = var[0] >= var[1] ? 0 : 1;
+    if (axis) axis = var[1] >= var[2] ? 1 : 2;
+    else axis = var[0] >= var[2] ? 0 : 2;
+    int a1 = axis == 0 ? 1 : 0;
+    int a2 = 3 - axis - a1;
+
+    /* projectSubMultiple (SapKernel.cu:151-213): quadrant of the centre on
+     * the two secondary axes about the origin (mPoint1 = mPoint2 = 0). */
+    uint32_t* grp[4];
+    uint32_t gn[4] = {0, 0, 0, 0};
+    for (int q = 0; q < 4; ++q) grp[q] = (uint32_t*)malloc((size_t)n * 4);
+    for (uint32_t i = 0; i < n; ++i) {
+        float y = cen[3 * (size_t)i + a1], z = cen[3 * (size_t)i + a2];
+        int q = (y >= 0.f && z >= 0.f) ? 1 : (y < 0.f && z >= 0.f) ? 2 : (y >= 0.f && z < 0.f) ? 3 : 0;
+        grp[q][gn[q]++] = i;
+    }
+    pvec all = {0, 0, 0};
+    for (int q = 0; q < 4; ++q) sweep_group(mode, mn, mx, axis, grp[q], gn[q], &all, nt);
+
+    /* Cross pass (cullCrossSphereMultiple :557-635, cullRelevantSphereMultiple
+     * :968-1059): maxR over objects straddling a plane, then every object
+     * within maxR of either plane is swept again without the quadrant key.
+     * For AABBs maxR is the largest secondary-axis width of a straddler. */
+    float maxR = 0.f;
+    for (uint32_t i = 0; i < n; ++i) {
+        float r, l1, h1, l2, h2;
+        if (mode == 0) {
+            l1 = mn[4 * (size_t)i + a1]; h1 = mx[4 * (size_t)i + a1];
+            l2 = mn[4 * (size_t)i + a2]; h2 = mx[4 * (size_t)i + a2];
+            float w1 = h1 - l1, w2 = h2 - l2;
+            r = w1 > w2 ? w1 : w2;
+        } else {
+            r = mn[4 * (size_t)i + 3];
+            float y = mn[4 * (size_t)i + a1], z = mn[4 * (size_t)i + a2];
+            l1 = y - r; h1 = y + r; l2 = z - r; h2 = z + r;
+        }
+        if ((h1 >= 0.f && l1 <= 0.f) || (h2 >= 0.f && l2 <= 0.f))
+            if (r > maxR) maxR = r;
+    }
+    uint32_t rn = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        float l1, h1, l2, h2;
+        if (mode == 0) {
+            l1 = mn[4 * (size_t)i + a1]; h1 = mx[4 * (size_t)i + a1];
+            l2 = mn[4 * (size_t)i + a2]; h2 = mx[4 * (size_t)i + a2];
+        } else {
+            float r = mn[4 * (size_t)i + 3];
+            float y = mn[4 * (size_t)i + a1], z = mn[4 * (size_t)i + a2];
+            l1 = y - r; h1 = y + r; l2 = z - r; h2 = z + r;
+        }
+        if ((h1 >= -maxR && l1 <= maxR) || (h2 >= -maxR && l2 <= maxR)) grp[0][rn++] = i;
+    }
+    if (rn > 0 && rn < n) sweep_group(mode, mn, mx, axis, grp[0], rn, &all, nt);
+    else if (rn == n) { /* every object is relevant: the quadrant sweeps are
+                           not enough, sweep them all together */
+        for (uint32_t i = 0; i < n; ++i) grp[0][i] = i;
+        sweep_group(mode, mn, mx, axis, grp[0], n, &all, nt);
+    }
+
+    /* Canonicalise: sort + unique (Sap.cpp:269-291, cullIndex :2249-2265). */
+    int idbits = 1;
+    while (idbits < 32 && ((uint64_t)1 << idbits) < n) ++idbits;
+    radix_sort_u64(all.p, all.n, 32 + ((idbits + 7) / 8) * 8);
+    int64_t u = 0;
+    for (size_t k = 0; k < all.n; ++k) {
+        if (k > 0 && all.p[k] == all.p[k - 1]) continue;
+        if (pairs && u < cap) {
+            pairs[2 * u] = (uint32_t)(all.p[k] >> 32);
+            pairs[2 * u + 1] = (uint32_t)all.p[k];
+        }
+        ++u;
+    }
+    for (int q = 0; q < 4; ++q) free(grp[q]);
+    free(cen);
+    free(all.p);
+    return u;
+}
+
+int64_t orc_both_directions(const uint32_t* pairs, int64_t np,
+                            int32_t* out_pairs, int32_t* out_entries) {
+    if (np <= 0) return 0;
+    uint32_t maxid = 0;
+    for (int64_t k = 0; k < 2 * np; ++k) if (pairs[k] > maxid) maxid = pairs[k];
+    size_t m = (size_t)maxid + 1;
+    int64_t* off = (int64_t*)calloc(m + 1, sizeof(int64_t));
+    for (int64_t k = 0; k < np; ++k) {
+        off[pairs[2 * k] + 1]++;
+        off[pairs[2 * k + 1] + 1]++;
+    }
+    int64_t ne = 0;
+    for (size_t a = 0; a < m; ++a) {
+        if (off[a + 1] > 0 && out_entries) out_entries[ne] = (int32_t)off[a];
+        if (off[a + 1] > 0) ++ne;
+        off[a + 1] += off[a];
+    }
+    /* stable fill in list order: rows come out sorted by second id */
+    int64_t* cur = (int64_t*)malloc(m * sizeof(int64_t));
+    memcpy(cur, off, m * sizeof(int64_t));
+    if (out_pairs) {
+        for (int64_t k = 0; k < np; ++k) {
+            uint32_t i = pairs[2 * k], j = pairs[2 * k + 1];
+            int64_t p = cur[i]++;
+            out_pairs[2 * p] = (int32_t)i;
+            out_pairs[2 * p + 1] = (int32_t)j;
+            p = cur[j]++;
+            out_pairs[2 * p] = (int32_t)j;
+            out_pairs[2 * p + 1] = (int32_t)i;
+        }
+    }
+    free(cur);
+    free(off);
+    return ne;
+}

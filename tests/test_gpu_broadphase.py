@@ -1,0 +1,158 @@
+"""GPU parity of the broadphase: the pair set, as a sorted (i < j) uint32
+list, must equal the oracle's bit for bit (the reference's own
+Aabb::overlaps golden lists, the O(n^2) brute force, and the CPU
+restatement of the reference SaP at full size)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+def to_dev(a, cuda):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a, np.float32)).to(cuda)
+
+
+def run_bp(sap, mn, mx, cuda, sorted=True, graph=False):
+    out = sap.broadphase(to_dev(mn, cuda), to_dev(mx, cuda) if mx is not None else None, sorted=sorted,
+                         graph=graph)
+    p = out.cpu().numpy().astype(np.uint32)
+    if not sorted:
+        p = p[np.lexsort((p[:, 1], p[:, 0]))]
+    return p
+
+
+@pytest.fixture(scope="module")
+def sap(cuda):
+    from gsap_gb300 import Sap
+    return Sap(1 << 16)
+
+
+def test_golden_reference_lists(sap, cuda):
+    g = np.load(os.path.join(GOLDEN, "aabb_bf_golden.npz"))
+    for name in g["names"]:
+        mn, mx, want = g[f"{name}__min"], g[f"{name}__max"], g[f"{name}__pairs"]
+        got = run_bp(sap, mn, mx, cuda)
+        assert np.array_equal(got, want), name
+        got = run_bp(sap, mn, mx, cuda, sorted=False)
+        assert np.array_equal(got, want), name
+
+
+@pytest.mark.parametrize("axis_mode", [0, 1])
+def test_uniform_16384_twenty_seeds(cuda, oracle_lib, axis_mode):
+    from gsap_gb300 import Sap, scenes
+    sap = Sap(16384, axis_mode=axis_mode)
+    for seed in range(20):
+        mn, mx = scenes.aabb_uniform(16384, seed)
+        want = oracle_lib.bf_aabb(mn, mx)
+        assert np.array_equal(run_bp(sap, mn, mx, cuda), want), seed
+
+
+@pytest.mark.parametrize("n", [2, 3, 31, 513, 4095, 4097, 9000])
+def test_odd_sizes_gauss(sap, cuda, oracle_lib, n):
+    from gsap_gb300 import scenes
+    c, h, _ = scenes.aabb_gauss_parts(n, seed=n, std=(10.0, 3.0, 1.0))
+    mn = np.concatenate([c - h, np.zeros((n, 1), np.float32)], 1)
+    mx = np.concatenate([c + h, np.zeros((n, 1), np.float32)], 1)
+    assert np.array_equal(run_bp(sap, mn, mx, cuda), oracle_lib.bf_aabb(mn, mx))
+
+
+def test_sphere_predicate(cuda, oracle_lib):
+    from gsap_gb300 import MODE_SPHERE, Sap
+    sap = Sap(20000, mode=MODE_SPHERE)
+    rng = np.random.default_rng(7)
+    for n, box in ((20000, 40.0), (3000, 8.0)):
+        s = np.concatenate([rng.uniform(0, box, (n, 3)), rng.uniform(0.1, 0.4, (n, 1))], 1).astype(np.float32)
+        # exactly touching and coincident spheres
+        s[1] = s[0]
+        s[3, :3] = s[2, :3] + np.float32([0.5, 0, 0]); s[2, 3] = 0.25; s[3, 3] = 0.25
+        got = run_bp(sap, s, None, cuda)
+        assert np.array_equal(got, oracle_lib.bf_sphere(s))
+
+
+def test_empty_and_single(sap, cuda):
+    for n in (0, 1):
+        mn = np.zeros((n, 4), np.float32)
+        assert len(run_bp(sap, mn, mn + 1, cuda)) == 0
+
+
+def test_graph_mode_and_repeat_calls(sap, cuda, oracle_lib):
+    from gsap_gb300 import scenes
+    mn, mx = scenes.aabb_uniform(16384, 5)
+    want = oracle_lib.bf_aabb(mn, mx)
+    for _ in range(3):
+        assert np.array_equal(run_bp(sap, mn, mx, cuda, graph=True), want)
+    assert np.array_equal(run_bp(sap, mn, mx, cuda), want)
+
+
+def test_capacity_error_reports_required_size(sap, cuda):
+    import torch
+    from gsap_gb300 import GsapError, _lib
+    g = np.load(os.path.join(GOLDEN, "aabb_bf_golden.npz"))
+    mn, mx = to_dev(g["identical_40__min"], cuda), to_dev(g["identical_40__max"], cuda)
+    pairs = torch.empty((100, 2), dtype=torch.int32, device=cuda)
+    import ctypes as C
+    cnt = C.c_uint64(0)
+    st = _lib.load().gsap_broadphase_aabb(sap.handle, mn.data_ptr(), mx.data_ptr(), 40, pairs.data_ptr(), 100,
+                                          None, C.byref(cnt), 0, None)
+    assert st == 2 and cnt.value == 780
+    # the handle still works afterwards
+    out = sap.broadphase(mn, mx)
+    assert len(out) == 780
+
+
+def test_nonfinite_input_is_reported(sap, cuda):
+    from gsap_gb300 import GsapError
+    mn = np.zeros((100, 4), np.float32)
+    mx = np.ones((100, 4), np.float32)
+    mn[17, 1] = np.nan
+    with pytest.raises(GsapError) as e:
+        run_bp(sap, mn, mx, cuda)
+    assert e.value.status == 5
+    mn[17, 1] = 0.0
+    assert len(run_bp(sap, mn, mx, cuda)) == 100 * 99 // 2
+
+
+def test_batched_matches_per_scene(cuda, oracle_lib):
+    import torch
+    from gsap_gb300 import Sap, scenes
+    mn, mx, off = scenes.batched_aabb(S=64, seed=3, lo=16, hi=3000)
+    n = len(mn)
+    bsap = Sap(n, max_scenes=64)
+    got = bsap.broadphase_batched(to_dev(mn, cuda), to_dev(mx, cuda),
+                                  torch.from_numpy(off.astype(np.int32)).to(cuda)).cpu().numpy().astype(np.uint32)
+    want = []
+    for s in range(64):
+        a, b = off[s], off[s + 1]
+        p = oracle_lib.bf_aabb(mn[a:b], mx[a:b]).astype(np.int64) + a
+        want.append(p)
+    want = np.concatenate(want).astype(np.uint32)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("axis_mode", [0, 1])
+def test_gauss_1m_against_cpu_sap(cuda, oracle_lib, axis_mode):
+    """Full-size 1,048,576-AABB case: equal to the CPU restatement of the
+    reference SaP, plus size-independent properties."""
+    from gsap_gb300 import Sap, scenes
+    c, h, R = scenes.aabb_gauss_parts(1 << 20, seed=0)
+    mn = np.concatenate([c - h, np.zeros((len(c), 1), np.float32)], 1)
+    mx = np.concatenate([c + h, np.zeros((len(c), 1), np.float32)], 1)
+    sap = Sap(1 << 20, axis_mode=axis_mode)
+    got = run_bp(sap, mn, mx, cuda)
+    # sorted, unique, i < j
+    assert np.all(got[:, 0] < got[:, 1])
+    key = got[:, 0].astype(np.uint64) << np.uint64(32) | got[:, 1].astype(np.uint64)
+    assert np.all(np.diff(key.astype(np.int64)) > 0)
+    # every pair overlaps
+    a, b = got[:, 0], got[:, 1]
+    assert np.all((mn[a, :3] <= mx[b, :3]) & (mn[b, :3] <= mx[a, :3]))
+    want = oracle_lib.sap_ref(0, mn, mx)
+    assert np.array_equal(got, want)
+    if axis_mode == 0:
+        ax = np.array(sap.scene_axes()["axes"][0])
+        assert abs(abs(ax @ R[:, 0]) - 1.0) < 1e-3

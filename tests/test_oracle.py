@@ -1,0 +1,129 @@
+"""CPU tests: the oracle against the golden vectors made by the reference's
+own code (tests/golden/make_golden.py), and its internal consistency."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+
+def load(name):
+    return np.load(os.path.join(GOLDEN, name), allow_pickle=False)
+
+
+def test_bf_aabb_matches_reference_overlaps(oracle_lib):
+    g = load("aabb_bf_golden.npz")
+    for name in g["names"]:
+        mn, mx, want = g[f"{name}__min"], g[f"{name}__max"], g[f"{name}__pairs"]
+        got = oracle_lib.bf_aabb(mn, mx) if len(mn) else np.zeros((0, 2), np.uint32)
+        assert np.array_equal(got, want), name
+
+
+def test_sap_restatement_matches_reference_overlaps(oracle_lib):
+    g = load("aabb_bf_golden.npz")
+    for name in g["names"]:
+        mn, mx, want = g[f"{name}__min"], g[f"{name}__max"], g[f"{name}__pairs"]
+        if len(mn) == 0:
+            continue
+        got = oracle_lib.sap_ref(0, mn, mx)
+        assert np.array_equal(got, want), name
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_sap_restatement_equals_brute_force(oracle_lib, seed):
+    rng = np.random.default_rng(seed)
+    n = 4000
+    R, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+    c = (rng.normal(size=(n, 3)) * np.array([30.0, 8.0, 3.0])) @ R.T
+    h = np.exp(rng.normal(-1.0, 0.5, (n, 3))).clip(0.05, 2.0)
+    mn, mx = (c - h).astype(np.float32), (c + h).astype(np.float32)
+    assert np.array_equal(oracle_lib.sap_ref(0, mn, mx), oracle_lib.bf_aabb(mn, mx))
+    sp = np.concatenate([c, h[:, :1]], 1).astype(np.float32)
+    assert np.array_equal(oracle_lib.sap_ref(1, sp), oracle_lib.bf_sphere(sp))
+
+
+def test_rb_reference_step_matches_reference_kernels(oracle_lib):
+    """The FP32 restatement reproduces the reference kernels bit for bit."""
+    g = load("rb_ref_step_golden.npz")
+    dt, spM, dpM, vmax, gy = (float(x) for x in g["params"])
+    s = {k[len("init__"):]: g[k].copy() for k in g.files if k.startswith("init__")}
+    for step in range(3):
+        npairs = oracle_lib.rb_step_ref(s, dt, spM, dpM, max_lin_vel=vmax, gravity_y=gy, floor_clamp=True,
+                                        torque_quirk=True, pair_loop_quirk=True)
+        assert npairs == int(g[f"step{step}__npairs"])
+        for k in ("pos", "quat", "lin_vel", "ang_vel", "p_pos", "p_vel", "p_force"):
+            assert np.array_equal(s[k], g[f"step{step}__{k}"]), (step, k)
+
+
+def test_both_direction_format_matches_demo_dump(oracle_lib):
+    """cudaPhysics/2_1024.txt: the reference's CPU broadphase dumps per frame
+    (pairs in both directions, pairEntries).  The oracle's both-direction
+    format reproduces each frame's pair set and entry offsets."""
+    g = load("demo_2_1024.npz")
+    for f in range(int(g["frames"])):
+        ij = g[f"f{f}__ij"]
+        n_pairs, n_ent = (int(x) for x in g[f"f{f}__counts"])
+        assert len(ij) == n_pairs
+        uniq = np.unique(np.sort(ij, axis=1), axis=0).astype(np.uint32)
+        both, ent = oracle_lib.both_directions(uniq)
+        assert len(both) == n_pairs
+        assert len(ent) == n_ent
+        assert set(map(tuple, both.tolist())) == set(map(tuple, ij.tolist()))
+        # entries are offsets of the first pair of every distinct first id
+        assert np.array_equal(ent, g[f"f{f}__entries"][:n_ent])
+
+
+def test_sphere_predicate_on_demo_dump(oracle_lib):
+    """Every pair of the dump overlaps under the squared strict test (the
+    dump prints 6 significant digits, so near-touching pairs are skipped)."""
+    g = load("demo_2_1024.npz")
+    checked = 0
+    for f in range(int(g["frames"])):
+        pi, pj = g[f"f{f}__pi"].astype(np.float64), g[f"f{f}__pj"].astype(np.float64)
+        d = np.linalg.norm(pi[:, :3] - pj[:, :3], axis=1)
+        r = pi[:, 3] + pj[:, 3]
+        clear = np.abs(d - r) > 1e-4 * r
+        assert np.all(d[clear] < r[clear])
+        pair = np.concatenate([pi, pj], 1).astype(np.float32).reshape(-1, 2, 4)
+        for a, b in pair[clear]:
+            got = oracle_lib.bf_sphere(np.stack([a, b]))
+            assert len(got) == 1
+            checked += 1
+    assert checked > 100
+
+
+def test_radix_sort_oracle_is_stable(oracle_lib):
+    rng = np.random.default_rng(3)
+    for bits in (8, 23, 24, 32):
+        k = rng.integers(0, 1 << min(bits, 31), 5000, dtype=np.uint64).astype(np.uint32)
+        k[::7] = k[0]
+        v = np.arange(len(k), dtype=np.uint32)
+        ks, vs = oracle_lib.radix_sort_u32(k, v, bits)
+        order = np.argsort(k & np.uint32((1 << bits) - 1 if bits < 32 else 0xFFFFFFFF), kind="stable")
+        assert np.array_equal(vs, order)
+
+
+def test_float_flip_orders_floats(oracle_lib):
+    x = np.array([-np.inf, -3.5, -1e-30, -0.0, 0.0, 1e-45, 2.0, np.inf], np.float32)
+    u = oracle_lib.float_flip(x)
+    assert np.all(np.diff(u.astype(np.int64)) >= 0)
+    assert oracle_lib.lib().orc_float_flip(2.0) == int(oracle_lib.float_flip(np.float32(2.0)).reshape(-1)[0])
+
+
+def test_cfg_f64_step_conserves_momentum_without_walls(oracle_lib):
+    """Two overlapping cubes, no gravity, walls far away: internal contact
+    forces cancel, so total linear momentum is unchanged."""
+    from gsap_gb300 import scenes
+    sc = scenes.cubes_in_box(2, box=1000.0, seed=0)
+    sc["pos"][0, :3] = [500.0, 500.0, 500.0]
+    sc["pos"][1, :3] = [501.2, 500.3, 500.1]
+    st = scenes.to_f64(sc)
+    p = dict(dt=1 / 600, k=2e4, eta=50.0, kt=0.1, gravity_y=0.0, box_lo=(0, 0, 0), box_hi=(1000, 1000, 1000))
+    m = 1.0 / st["inv_mass"]
+    p0 = (st["lin_vel"][:, :3] * m[:, None]).sum(0)
+    for _ in range(5):
+        oracle_lib.rb_step_cfg_f64(st, p)
+    p1 = (st["lin_vel"][:, :3] * m[:, None]).sum(0)
+    assert np.allclose(p0, p1, atol=1e-9)
+    assert np.abs(st["lin_vel"][:, :3]).max() > 0  # they did collide
