@@ -20,8 +20,10 @@ LIB = os.path.join(HERE, "libgsap.so")
 INC = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-         "-Xcompiler", "-Wall", "-diag-suppress", "177"]
+# Host code: no FMA contraction, so host-side float arithmetic (the quaternion
+# normalisation on upload) gives the same bits on x86 and aarch64.
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+         "--expt-relaxed-constexpr", "-Xcompiler", "-Wall", "-diag-suppress", "177"]
 # The reference-model rigid-body kernels round every product and sum
 # separately (no FMA contraction), as the reference's source order does.
 PER_FILE = {"rigid_ref.cu": ["-fmad=false"]}

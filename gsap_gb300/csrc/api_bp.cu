@@ -15,6 +15,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "../../include/gsap.h"
 #include "../../include/gsap_debug.h"
@@ -85,15 +86,21 @@ struct GraphKey {
     bool operator==(const GraphKey& o) const { return memcmp(this, &o, sizeof(*this)) == 0; }
 };
 
+struct GraphEntry {
+    GraphKey key;
+    cudaGraphExec_t exec;
+    uint64_t last_use;
+};
+constexpr size_t kMaxGraphs = 128;  // cached pipeline graphs per handle (LRU)
+
 struct gsap_sap {
     gsap_config cfg;
     BpScratch s;
     int device;
     uint32_t* h_ctrl;   // pinned copy of the head of the control block
     cudaStream_t cap_stream;
-    cudaGraphExec_t gexec;
-    GraphKey gkey;
-    bool has_graph;
+    std::vector<GraphEntry>* graphs;
+    uint64_t use_clock;
     bool timing;
     cudaEvent_t ev[8];
     float stage_ms[6];
@@ -103,11 +110,16 @@ struct gsap_sap {
 static void free_scratch(gsap_sap* h) {
     BpScratch& s = h->s;
     void* ptrs[] = {s.ctrl, s.scenes, s.partials, s.scene_done, s.work_start, s.objcell, s.objscene,
-                    s.keys[0], s.keys[1], s.vals[0], s.vals[1], s.status, s.rowcnt, s.rowoff, s.tmp_pairs};
+                    s.keys[0], s.keys[1], s.vals[0], s.vals[1], s.status, s.rowcnt, s.rowoff, s.tmp_pairs,
+                    s.smin, s.smax, s.scell, s.longrows};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (h->h_ctrl) cudaFreeHost(h->h_ctrl);
-    if (h->has_graph) cudaGraphExecDestroy(h->gexec);
+    if (h->graphs) {
+        for (auto& g : *h->graphs) cudaGraphExecDestroy(g.exec);
+        delete h->graphs;
+        h->graphs = nullptr;
+    }
     if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
     for (auto& e : h->ev)
         if (e) cudaEventDestroy(e);
@@ -130,6 +142,7 @@ extern "C" gsap_sap* gsap_sap_create(uint32_t max_n, const gsap_config* cfg) {
     gsap_sap* h = new gsap_sap();
     memset(h, 0, sizeof(*h));
     h->cfg = c;
+    h->graphs = new std::vector<GraphEntry>();
     cudaGetDevice(&h->device);
     BpScratch& s = h->s;
     s.max_n = max_n;
@@ -157,6 +170,10 @@ extern "C" gsap_sap* gsap_sap_create(uint32_t max_n, const gsap_config* cfg) {
         A((void**)&s.vals[k], 4ull * ecap);
     }
     A((void**)&s.status, 8ull * s.status_words);
+    A((void**)&s.smin, 16ull * ecap);
+    A((void**)&s.smax, 16ull * ecap);
+    A((void**)&s.scell, 4ull * ecap);
+    A((void**)&s.longrows, 4ull * (max_n + 1));
     A((void**)&s.rowcnt, 4ull * (max_n + 1));
     A((void**)&s.rowoff, 4ull * (max_n + 1));
     A((void**)&s.tmp_pairs, 8ull * s.pair_cap_internal);
@@ -234,9 +251,10 @@ static gsap_status record(gsap_sap* h, const Call& c, cudaStream_t st, bool time
     mark();
     const uint32_t* count = &s.ctrl->entry_count;
     int src = 0;
+    SortGather gather{c.mn, c.mode == GSAP_MODE_AABB ? c.mx : nullptr, s.objcell, s.smin, s.smax, s.scell};
     for (int p = 0; p < passes; ++p) {
         CK(launch_sort_pass(s, p, passes, s.keys[src], s.vals[src], s.keys[src ^ 1], s.vals[src ^ 1], count,
-                            s.entry_cap, a.spin_limit, st));
+                            s.entry_cap, a.spin_limit, st, p == passes - 1 ? &gather : nullptr));
         src ^= 1;
     }
     mark();
@@ -266,10 +284,17 @@ static gsap_status run(gsap_sap* h, const Call& c, cudaStream_t st) {
     k.mn = c.mn; k.mx = c.mx; k.off = c.off; k.pairs = c.pairs; k.dcount = c.d_count; k.entries = c.entries;
     k.n = c.n; k.S = c.S; k.flags = c.flags; k.mode = (uint32_t)c.mode; k.both = (uint32_t)c.both;
     k.cap = c.cap; k.ecap = c.ecap;
-    if (!h->has_graph || !(h->gkey == k)) {
-        if (h->has_graph) {
-            cudaGraphExecDestroy(h->gexec);
-            h->has_graph = false;
+    // LRU cache of captured pipelines, one per (inputs, outputs, sizes, flags)
+    GraphEntry* hit = nullptr;
+    for (auto& g : *h->graphs)
+        if (g.key == k) { hit = &g; break; }
+    if (!hit) {
+        if (h->graphs->size() >= kMaxGraphs) {
+            size_t old = 0;
+            for (size_t i = 1; i < h->graphs->size(); ++i)
+                if ((*h->graphs)[i].last_use < (*h->graphs)[old].last_use) old = i;
+            cudaGraphExecDestroy((*h->graphs)[old].exec);
+            h->graphs->erase(h->graphs->begin() + old);
         }
         cudaGraph_t g;
         CK(cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal));
@@ -277,13 +302,16 @@ static gsap_status run(gsap_sap* h, const Call& c, cudaStream_t st) {
         cudaError_t e = cudaStreamEndCapture(h->cap_stream, &g);
         if (r != GSAP_OK) return r;
         if (e != cudaSuccess) return fail(GSAP_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
-        e = cudaGraphInstantiate(&h->gexec, g, 0);
+        GraphEntry ent;
+        ent.key = k;
+        e = cudaGraphInstantiate(&ent.exec, g, 0);
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return fail(GSAP_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
-        h->has_graph = true;
-        h->gkey = k;
+        h->graphs->push_back(ent);
+        hit = &h->graphs->back();
     }
-    CK(cudaGraphLaunch(h->gexec, st));
+    hit->last_use = ++h->use_clock;
+    CK(cudaGraphLaunch(hit->exec, st));
     return GSAP_OK;
 }
 
@@ -497,6 +525,22 @@ extern "C" int gsap_debug_scene_solve(const double* sums18, const double* hmax3,
     for (int k = 0; k < 3; ++k) { out17[9 + k] = sc.eig[k]; out17[12 + k] = sc.mean[k]; }
     out17[15] = sc.G2;
     out17[16] = sc.G3;
+    return 0;
+}
+
+extern "C" int gsap_debug_stats(gsap_sap* h, uint64_t* out8, void* stream) {
+    if (!h || !out8) return -1;
+    Ctrl c;
+    if (cudaMemcpyAsync(&c, h->s.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, (cudaStream_t)stream) != cudaSuccess) return -1;
+    if (cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess) return -1;
+    out8[0] = c.entry_count;
+    out8[1] = c.tests;
+    out8[2] = c.pair_count;
+    out8[3] = c.total_buckets;
+    out8[4] = c.qbits;
+    out8[5] = c.long_rows;
+    out8[6] = c.key_bits;
+    out8[7] = c.error;
     return 0;
 }
 

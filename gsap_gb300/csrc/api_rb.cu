@@ -31,6 +31,8 @@ struct gsap_rb {
     float* inv_mass;
     float4* inv_inertia;  // 3 rows per body
     float4 *p_pos, *p_vel, *p_force;
+    float4* p_rel;        // config model: body-relative particle offsets (w = radius)
+    bool abs_stale;       // config model: p_pos must be rebuilt from p_rel before a read
     float* p_mass;
     float4* ref_pos;      // kMaxParticlesPerBody * kMaxShapes
     float* ref_mass;
@@ -48,7 +50,7 @@ struct gsap_rb {
 
 static void rb_free(gsap_rb* h) {
     void* p[] = {h->pos, h->quat, h->lin, h->ang, h->shape, h->pstart, h->npart, h->p_body, h->inv_mass,
-                 h->inv_inertia, h->p_pos, h->p_vel, h->p_force, h->p_mass, h->ref_pos, h->ref_mass, h->shape_inv,
+                 h->inv_inertia, h->p_pos, h->p_vel, h->p_force, h->p_rel, h->p_mass, h->ref_pos, h->ref_mass, h->shape_inv,
                  h->pairs, h->entries, h->bmin, h->bmax, h->body_pairs, h->scene_off};
     for (void* q : p)
         if (q) cudaFree(q);
@@ -76,6 +78,7 @@ extern "C" gsap_rb* gsap_rb_create(int32_t max_bodies, int32_t max_particles, in
     A((void**)&h->p_body, 4 * Pn);
     A((void**)&h->inv_mass, 4 * B); A((void**)&h->inv_inertia, 48 * B);
     A((void**)&h->p_pos, 16 * Pn); A((void**)&h->p_vel, 16 * Pn); A((void**)&h->p_force, 16 * Pn);
+    A((void**)&h->p_rel, 16 * Pn);
     A((void**)&h->p_mass, 4 * Pn);
     A((void**)&h->ref_pos, 16ull * kMaxParticlesPerBody * kMaxShapes);
     A((void**)&h->ref_mass, 4ull * kMaxParticlesPerBody * kMaxShapes);
@@ -115,7 +118,8 @@ extern "C" gsap_status gsap_rb_set_body_data(gsap_rb* h, const gsap_body_data* d
     if (nb > 0 && (!d->pos || !d->quat || !d->lin_vel || !d->ang_vel || !d->shape_idx || !d->p_start ||
                    !d->n_part || !d->inv_mass || !d->inv_inertia))
         return set_error(GSAP_ERR_INVALID, "null body array");
-    // quaternions are normalised on upload (setRbData, ParticleRigidBody.cpp:82-86)
+    // quaternions are normalised on upload (setRbData, ParticleRigidBody.cpp:82-86):
+    // q *= 1 / sqrtf(dot4(q, q)), sums left to right, one rounding per operation
     std::vector<float> q(d->quat, d->quat + 4 * (size_t)nb);
     for (int b = 0; b < nb; ++b) {
         float* v = &q[4 * b];
@@ -216,9 +220,9 @@ extern "C" gsap_status gsap_rb_update_particle_data(gsap_rb* h, void* stream) {
     if (!h) return set_error(GSAP_ERR_INVALID, "null handle");
     cudaStream_t st = (cudaStream_t)stream;
     if (h->cp.model == GSAP_CONTACT_CONFIG) {
-        RCK(rb_place_cfg(h->pos, h->quat, h->lin, h->ang, h->shape, h->pstart, h->p_body, h->ref_pos, h->p_pos,
-                         h->p_vel, h->n_particles, st));
-        // particle masses as in the reference placement
+        RCK(rb_place_cfg(h->quat, h->lin, h->ang, h->shape, h->pstart, h->p_body, h->ref_pos, h->p_rel, h->p_vel,
+                         h->n_particles, st));
+        h->abs_stale = true;
         return GSAP_OK;
     }
     RCK(rb_place_ref(h->pos, h->quat, h->lin, h->ang, h->shape, h->pstart, h->npart, h->p_body, h->ref_pos,
@@ -241,7 +245,7 @@ extern "C" gsap_status gsap_rb_compute_forces(gsap_rb* h, float dt, void* stream
                            h->n_particles, dt, st));
     RCK(rb_pair_force_ref(h->p_pos, h->p_vel, h->pairs, h->entries, h->num_pairs, h->num_entries, h->num_entries,
                           nullptr, nullptr, h->p_mass, h->cp.sp_multip, h->cp.dp_multip, h->p_force, dt,
-                          (int)h->cp.pair_loop_quirk, st));
+                          (int)h->cp.pair_loop_quirk, h->max_pairs, st));
     return GSAP_OK;
 }
 
@@ -262,7 +266,21 @@ extern "C" gsap_status gsap_rb_update_velocity(gsap_rb* h, float dt, void* strea
 
 extern "C" int32_t* gsap_rb_pairs(gsap_rb* h) { return h ? (int32_t*)h->pairs : nullptr; }
 extern "C" int32_t* gsap_rb_pair_entries(gsap_rb* h) { return h ? h->entries : nullptr; }
-extern "C" float* gsap_rb_particle_pos(gsap_rb* h) { return h ? (float*)h->p_pos : nullptr; }
+// Config model: absolute particle positions are rebuilt from the body poses
+// and body-relative offsets before they are handed out.
+static void refresh_abs(gsap_rb* h, cudaStream_t st) {
+    if (h->cp.model == GSAP_CONTACT_CONFIG && h->abs_stale) {
+        rb_abs_pos(h->pos, h->p_body, h->p_rel, h->p_pos, h->n_particles, st);
+        cudaStreamSynchronize(st);
+        h->abs_stale = false;
+    }
+}
+
+extern "C" float* gsap_rb_particle_pos(gsap_rb* h) {
+    if (!h) return nullptr;
+    refresh_abs(h, nullptr);
+    return (float*)h->p_pos;
+}
 extern "C" float* gsap_rb_particle_vel(gsap_rb* h) { return h ? (float*)h->p_vel : nullptr; }
 extern "C" float* gsap_rb_particle_force(gsap_rb* h) { return h ? (float*)h->p_force : nullptr; }
 
@@ -292,21 +310,22 @@ extern "C" gsap_status gsap_rb_step(gsap_rb* h, gsap_sap* bp, float dt, void* st
                                h->n_particles, dt, st));
         RCK(rb_pair_force_ref(h->p_pos, h->p_vel, h->pairs, h->entries, 0, 0, h->n_particles, dc.num_pairs,
                               dc.num_entries, h->p_mass, h->cp.sp_multip, h->cp.dp_multip, h->p_force, dt,
-                              (int)h->cp.pair_loop_quirk, st));
+                              (int)h->cp.pair_loop_quirk, h->max_pairs, st));
         return gsap_rb_update_velocity(h, dt, stream);
     }
     // config model
     CfgParams p = cfg_of(h, dt);
     RCK(rb_integrate_cfg(h->pos, h->quat, h->lin, h->ang, p, h->n_bodies, st));
-    RCK(rb_place_cfg(h->pos, h->quat, h->lin, h->ang, h->shape, h->pstart, h->p_body, h->ref_pos, h->p_pos, h->p_vel,
+    RCK(rb_place_cfg(h->quat, h->lin, h->ang, h->shape, h->pstart, h->p_body, h->ref_pos, h->p_rel, h->p_vel,
                      h->n_particles, st));
-    RCK(rb_body_aabb(h->p_pos, h->pstart, h->npart, h->bmin, h->bmax, h->n_bodies, st));
+    h->abs_stale = true;
+    RCK(rb_body_aabb(h->pos, h->p_rel, h->pstart, h->npart, h->bmin, h->bmax, h->n_bodies, st));
     BpDeviceCounts dc;
     r = bp_both_async(bp, GSAP_MODE_AABB, h->bmin, h->bmax, h->scene_off, h->num_scenes ? h->num_scenes : 1,
                       (uint32_t)h->n_bodies, h->body_pairs, h->body_pair_cap, nullptr, 0, st, &dc);
     if (r != GSAP_OK) return r;
-    RCK(rb_forces_cfg(h->p_pos, h->p_vel, h->p_body, h->pstart, h->npart, h->body_pairs, dc.rowoff, p, h->p_force,
-                      h->n_particles, st));
+    RCK(rb_forces_cfg(h->pos, h->p_rel, h->p_vel, h->p_body, h->pstart, h->npart, h->body_pairs, dc.rowoff,
+                      h->body_pair_cap, p, h->p_force, h->n_particles, st));
     RCK(rb_update_cfg(h->lin, h->ang, h->quat, h->inv_mass, h->shape, h->pstart, h->npart, h->ref_pos, h->shape_inv,
                       h->p_force, p, h->n_bodies, st));
     return GSAP_OK;
@@ -343,6 +362,7 @@ extern "C" gsap_status gsap_rb_copy_out(gsap_rb* h, int32_t which, void* dst, ui
     if (!src) return set_error(GSAP_ERR_INVALID, "unknown array");
     if (bytes > cap) return set_error(GSAP_ERR_CAPACITY, "copy larger than the array");
     cudaStream_t st = (cudaStream_t)stream;
+    if (which == GSAP_RB_PARTICLE_POS) refresh_abs(h, st);
     RCK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
     RCK(cudaStreamSynchronize(st));
     return GSAP_OK;
@@ -357,6 +377,7 @@ extern "C" gsap_status gsap_rb_copy_in(gsap_rb* h, int32_t which, const void* sr
     cudaStream_t st = (cudaStream_t)stream;
     RCK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
     RCK(cudaStreamSynchronize(st));
+    if (which == GSAP_RB_PARTICLE_POS) h->abs_stale = false;
     return GSAP_OK;
 }
 
@@ -413,7 +434,7 @@ extern "C" gsap_status gsap_k_compute_force_on_particles(const float* p_pos, con
                                                          float* p_force, float dt, int32_t quirk, void* stream) {
     RCK(rb_pair_force_ref((const float4*)p_pos, (const float4*)p_vel, (const int2*)pairs, entries, num_pairs,
                           num_entries, num_entries, nullptr, nullptr, p_mass, sp, dp, (float4*)p_force, dt, quirk,
-                          (cudaStream_t)stream));
+                          num_pairs, (cudaStream_t)stream));
     return GSAP_OK;
 }
 

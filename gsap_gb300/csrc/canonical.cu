@@ -111,32 +111,95 @@ __global__ void __launch_bounds__(kThreads) k_scatter(BpScratch S, const uint2* 
     }
 }
 
-// Sort every row by its second id (rows are short: insertion sort in
-// registers up to 32, in place beyond).
+// Bitonic sorting network over N registers (every index is a compile-time
+// constant after unrolling, so v[] stays in registers).
+template <int N>
+__device__ __forceinline__ void bitonic_regs(uint32_t (&v)[N]) {
+#pragma unroll
+    for (int k = 2; k <= N; k <<= 1)
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1)
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const bool up = (i & k) == 0;
+                    uint32_t a = v[i], b = v[l];
+                    bool sw = up ? (a > b) : (a < b);
+                    v[i] = sw ? b : a;
+                    v[l] = sw ? a : b;
+                }
+            }
+}
+
+template <int N>
+__device__ __forceinline__ void sort_row(uint2* out, uint64_t b, uint32_t len) {
+    uint32_t v[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) v[k] = ((uint32_t)k < len) ? out[b + k].y : 0xFFFFFFFFu;
+    bitonic_regs<N>(v);
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+        if ((uint32_t)k < len) out[b + k].y = v[k];
+}
+
+// Sort every row by its second id: one thread per row with a register
+// network for rows of up to 32 pairs (rows average ~5-11 pairs); longer
+// rows are queued for k_rowsort_long.
 __global__ void __launch_bounds__(kThreads) k_rowsort(BpScratch S, uint2* out, uint64_t out_cap, uint32_t n) {
     for (uint32_t r = blockIdx.x * kThreads + threadIdx.x; r < n; r += gridDim.x * kThreads) {
         uint64_t b = S.rowoff[r], e = S.rowoff[r + 1];
         if (e > out_cap) e = out_cap;
         if (e <= b + 1) continue;
         uint32_t len = (uint32_t)(e - b);
-        if (len <= 32) {
-            uint32_t y[32];
-            for (uint32_t k = 0; k < len; ++k) y[k] = out[b + k].y;
-            for (uint32_t k = 1; k < len; ++k) {
-                uint32_t v = y[k];
-                int m = (int)k - 1;
-                while (m >= 0 && y[m] > v) { y[m + 1] = y[m]; --m; }
-                y[m + 1] = v;
-            }
-            for (uint32_t k = 0; k < len; ++k) out[b + k].y = y[k];
+        if (len <= 8) sort_row<8>(out, b, len);
+        else if (len <= 16) sort_row<16>(out, b, len);
+        else if (len <= 32) sort_row<32>(out, b, len);
+        else S.longrows[atomicAdd(&S.ctrl->long_rows, 1u)] = r;
+    }
+}
+
+constexpr int kLongRow = 4096;
+
+// One CTA per long row: bitonic sort in shared memory (rows up to 4096
+// pairs), odd-even transposition in place beyond that.
+__global__ void __launch_bounds__(kThreads) k_rowsort_long(BpScratch S, uint2* out, uint64_t out_cap) {
+    __shared__ uint32_t s[kLongRow];
+    const uint32_t nlong = S.ctrl->long_rows;
+    for (uint32_t q = blockIdx.x; q < nlong; q += gridDim.x) {
+        const uint32_t r = S.longrows[q];
+        uint64_t b = S.rowoff[r], e = S.rowoff[r + 1];
+        if (e > out_cap) e = out_cap;
+        if (e <= b + 1) continue;
+        const uint32_t len = (uint32_t)(e - b);
+        if (len <= (uint32_t)kLongRow) {
+            uint32_t P = 32;
+            while (P < len) P <<= 1;
+            for (uint32_t k = threadIdx.x; k < P; k += kThreads) s[k] = k < len ? out[b + k].y : 0xFFFFFFFFu;
+            __syncthreads();
+            for (uint32_t k = 2; k <= P; k <<= 1)
+                for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                    for (uint32_t i = threadIdx.x; i < P; i += kThreads) {
+                        uint32_t l = i ^ j;
+                        if (l > i) {
+                            bool up = (i & k) == 0;
+                            uint32_t a = s[i], c = s[l];
+                            if (up ? (a > c) : (a < c)) { s[i] = c; s[l] = a; }
+                        }
+                    }
+                    __syncthreads();
+                }
+            for (uint32_t k = threadIdx.x; k < len; k += kThreads) out[b + k].y = s[k];
         } else {
-            for (uint64_t k = b + 1; k < e; ++k) {
-                uint32_t v = out[k].y;
-                uint64_t m = k;
-                while (m > b && out[m - 1].y > v) { out[m].y = out[m - 1].y; --m; }
-                out[m].y = v;
+            for (uint32_t phase = 0; phase < len; ++phase) {
+                for (uint32_t i = 2 * threadIdx.x + (phase & 1); i + 1 < len; i += 2 * kThreads) {
+                    uint32_t a = out[b + i].y, c = out[b + i + 1].y;
+                    if (a > c) { out[b + i].y = c; out[b + i + 1].y = a; }
+                }
+                __syncthreads();
             }
         }
+        __syncthreads();
     }
 }
 
@@ -147,6 +210,7 @@ cudaError_t launch_canonical(const BpScratch& s, uint32_t n, const uint2* in_pai
     k_scan<0><<<grid, kThreads, 0, st>>>(s, s.rowcnt, s.rowoff, nullptr, 0, n, 5, spin);
     k_scatter<<<grid * 2, kThreads, 0, st>>>(s, in_pairs, in_cap, out_pairs, out_cap, both);
     k_rowsort<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(s, out_pairs, out_cap, n);
+    k_rowsort_long<<<sm_count() * 2, kThreads, 0, st>>>(s, out_pairs, out_cap);
     if (both && entries) k_scan<1><<<grid, kThreads, 0, st>>>(s, s.rowoff, nullptr, entries, entry_cap, n, 6, spin);
     return cudaGetLastError();
 }

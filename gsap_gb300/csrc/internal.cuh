@@ -44,7 +44,8 @@ struct Ctrl {
     uint32_t scan_total;      // total of the last look-back scan
     uint32_t scan_ctr;        // tile counter of the look-back scan
     uint32_t sort_n;          // key count of a standalone sort
-    uint32_t pad;
+    uint32_t long_rows;       // canonical output: rows longer than the register sort
+    unsigned long long tests; // sweep: candidate pairs tested (diagnostics)
     uint32_t hist[kMaxPasses][256];
 };
 
@@ -86,6 +87,10 @@ struct BpScratch {
     uint32_t* keys[2];
     uint32_t* vals[2];
     uint64_t* status;          // look-back words
+    float4* smin;              // sweep entries in sorted order: bounds (sphere in smin)
+    float4* smax;
+    uint32_t* scell;           // sorted entries: (c2lo << 16) | c3lo of the object
+    uint32_t* longrows;        // canonical output: ids of rows longer than 32
     uint32_t* rowcnt;          // per object pair counts (canonical output)
     uint32_t* rowoff;          // exclusive offsets, n+1
     uint32_t* tmp_pairs;       // unsorted pairs before canonicalisation
@@ -116,9 +121,20 @@ struct BpArgs {
 cudaError_t launch_plan(const BpScratch& s, const BpArgs& a, cudaStream_t st);
 cudaError_t launch_pca(const BpScratch& s, const BpArgs& a, cudaStream_t st);
 cudaError_t launch_project(const BpScratch& s, const BpArgs& a, int passes, cudaStream_t st);
+// Gather epilogue of the last sort pass: entry g also gets the bounds and
+// lower-corner cell of its object, so the sweep reads candidates in order.
+struct SortGather {
+    const float4* mn;
+    const float4* mx;          // nullptr in sphere mode
+    const uint32_t* objcell;
+    float4* smin;
+    float4* smax;
+    uint32_t* scell;
+};
 cudaError_t launch_sort_pass(const BpScratch& s, int pass, int passes, const uint32_t* kin,
                              const uint32_t* vin, uint32_t* kout, uint32_t* vout,
-                             const uint32_t* count_ptr, uint64_t cap, uint32_t spin, cudaStream_t st);
+                             const uint32_t* count_ptr, uint64_t cap, uint32_t spin, cudaStream_t st,
+                             const SortGather* gather = nullptr);
 cudaError_t launch_sort_prep(const BpScratch& s, const uint32_t* keys, const uint32_t* count_ptr,
                              uint32_t n, int passes, cudaStream_t st);
 cudaError_t launch_sweep(const BpScratch& s, const BpArgs& a, const uint32_t* keys, const uint32_t* vals,

@@ -229,6 +229,8 @@ __global__ void __launch_bounds__(kThreads) k_pca(BpScratch S, BpArgs A, uint64_
         C->sweep_ctr = 0;
         C->scan_ctr = 0;
         C->scan_total = 0;
+        C->long_rows = 0;
+        C->tests = 0ull;
         C->epoch = C->epoch + 1u;
         C->scenes_done = 0;
     }

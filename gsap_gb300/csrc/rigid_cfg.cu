@@ -17,6 +17,14 @@
 // neighbour-id order, and writes its force once, no read-modify-write); one
 // thread per body for the body AABB and for the compensated (two-sum)
 // per-body force / torque reduction fused with the velocity update.
+//
+// Precision: particles are kept as body-relative offsets r = R ref (|r| <= a
+// few units) next to the FP32 body positions x.  A particle-particle vector
+// is formed as (x_b - x_a) + (r_j - r_i): the body difference is exact or
+// nearly so for touching bodies, so the penetration depth keeps ~1e-7
+// absolute accuracy instead of the ~4e-6 an absolute FP32 coordinate near
+// 100 would give it.  Absolute particle positions are produced only when the
+// caller reads them.
 #include "internal.cuh"
 #include "rigid.cuh"
 
@@ -58,9 +66,9 @@ __global__ void k_integrate_cfg(float4* pos, float4* quat, float4* lin, const fl
     pos[b] = x;
 }
 
-__global__ void k_place_cfg(const float4* pos, const float4* quat, const float4* lin, const float4* ang,
-                            const int* shape, const int* pstart, const int* p_body, const float4* ref_pos,
-                            float4* p_pos, float4* p_vel, int np) {
+__global__ void k_place_cfg(const float4* quat, const float4* lin, const float4* ang, const int* shape,
+                            const int* pstart, const int* p_body, const float4* ref_pos, float4* p_rel,
+                            float4* p_vel, int np) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= np) return;
     int b = p_body[i];
@@ -68,23 +76,37 @@ __global__ void k_place_cfg(const float4* pos, const float4* quat, const float4*
     float3 R[3];
     qrows(quat[b], R);
     float3 r = mv(R, make_float3(ref.x, ref.y, ref.z));
-    float4 x = pos[b], v = lin[b], w = ang[b];
+    float4 v = lin[b], w = ang[b];
     float3 wr = cross3(make_float3(w.x, w.y, w.z), r);
-    p_pos[i] = make_float4(x.x + r.x, x.y + r.y, x.z + r.z, ref.w);
+    p_rel[i] = make_float4(r.x, r.y, r.z, ref.w);
     p_vel[i] = make_float4(v.x + wr.x, v.y + wr.y, v.z + wr.z, 0.f);
 }
 
-__global__ void k_body_aabb(const float4* p_pos, const int* pstart, const int* npart, float4* bmin, float4* bmax,
-                            int n) {
+// absolute particle positions (readback only)
+__global__ void k_abs_pos(const float4* pos, const int* p_body, const float4* p_rel, float4* p_pos, int np) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    float4 x = pos[p_body[i]], r = p_rel[i];
+    p_pos[i] = make_float4(x.x + r.x, x.y + r.y, x.z + r.z, r.w);
+}
+
+__global__ void k_body_aabb(const float4* pos, const float4* p_rel, const int* pstart, const int* npart,
+                            float4* bmin, float4* bmax, int n) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= n) return;
     int s = pstart[b], m = npart[b];
+    float4 x = pos[b];
     float3 lo = make_float3(INFINITY, INFINITY, INFINITY), hi = make_float3(-INFINITY, -INFINITY, -INFINITY);
     for (int k = 0; k < m; ++k) {
-        float4 p = p_pos[s + k];
-        float r = fabsf(p.w);
-        lo.x = fminf(lo.x, __fsub_rd(p.x, r)); lo.y = fminf(lo.y, __fsub_rd(p.y, r)); lo.z = fminf(lo.z, __fsub_rd(p.z, r));
-        hi.x = fmaxf(hi.x, __fadd_ru(p.x, r)); hi.y = fmaxf(hi.y, __fadd_ru(p.y, r)); hi.z = fmaxf(hi.z, __fadd_ru(p.z, r));
+        float4 r = p_rel[s + k];
+        float rad = fabsf(r.w);
+        // x + r -/+ rad, rounded outward at every step
+        lo.x = fminf(lo.x, __fsub_rd(__fadd_rd(x.x, r.x), rad));
+        lo.y = fminf(lo.y, __fsub_rd(__fadd_rd(x.y, r.y), rad));
+        lo.z = fminf(lo.z, __fsub_rd(__fadd_rd(x.z, r.z), rad));
+        hi.x = fmaxf(hi.x, __fadd_ru(__fadd_ru(x.x, r.x), rad));
+        hi.y = fmaxf(hi.y, __fadd_ru(__fadd_ru(x.y, r.y), rad));
+        hi.z = fmaxf(hi.z, __fadd_ru(__fadd_ru(x.z, r.z), rad));
     }
     if (m == 0) { lo = make_float3(0.f, 0.f, 0.f); hi = make_float3(-1.f, -1.f, -1.f); }
     bmin[b] = make_float4(lo.x, lo.y, lo.z, 0.f);
@@ -100,39 +122,44 @@ __device__ __forceinline__ void contact(const CfgParams& p, float3 n, float pen,
     f.z += ks * n.z + kt * (v.z - vn * n.z);
 }
 
-__global__ void __launch_bounds__(256) k_forces_cfg(const float4* __restrict__ p_pos, const float4* __restrict__ p_vel,
-                                                    const int* p_body, const int* pstart, const int* npart,
-                                                    const uint2* body_pairs, const uint32_t* rowoff, CfgParams p,
+__global__ void __launch_bounds__(256) k_forces_cfg(const float4* __restrict__ pos, const float4* __restrict__ p_rel,
+                                                    const float4* __restrict__ p_vel, const int* p_body,
+                                                    const int* pstart, const int* npart, const uint2* body_pairs,
+                                                    const uint32_t* rowoff, uint64_t pair_cap, CfgParams p,
                                                     float4* p_force, int np) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= np) return;
-    float4 ip = p_pos[i], iv = p_vel[i];
+    const int a = p_body[i];
+    const float4 xa = pos[a], ri = p_rel[i], iv = p_vel[i];
     float3 f = make_float3(0.f, 0.f, 0.f);
     float3 vw = make_float3(-iv.x, -iv.y, -iv.z);
-    const float pc[3] = {ip.x, ip.y, ip.z};
+    const float xs[3] = {xa.x, xa.y, xa.z}, rs[3] = {ri.x, ri.y, ri.z};
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        float pen_lo = ip.w - (pc[a] - p.lo[a]);
-        float pen_hi = ip.w - (p.hi[a] - pc[a]);
+    for (int k = 0; k < 3; ++k) {
+        // distance to the walls: (x - lo) + r and (hi - x) - r
+        float pen_lo = ri.w - ((xs[k] - p.lo[k]) + rs[k]);
+        float pen_hi = ri.w - ((p.hi[k] - xs[k]) - rs[k]);
         if (pen_lo > 0.f) {
-            float3 n = make_float3(a == 0 ? -1.f : 0.f, a == 1 ? -1.f : 0.f, a == 2 ? -1.f : 0.f);
+            float3 n = make_float3(k == 0 ? -1.f : 0.f, k == 1 ? -1.f : 0.f, k == 2 ? -1.f : 0.f);
             contact(p, n, pen_lo, vw, f);
         }
         if (pen_hi > 0.f) {
-            float3 n = make_float3(a == 0 ? 1.f : 0.f, a == 1 ? 1.f : 0.f, a == 2 ? 1.f : 0.f);
+            float3 n = make_float3(k == 0 ? 1.f : 0.f, k == 1 ? 1.f : 0.f, k == 2 ? 1.f : 0.f);
             contact(p, n, pen_hi, vw, f);
         }
     }
-    int a = p_body[i];
     uint32_t e0 = rowoff[a], e1 = rowoff[a + 1];
+    if (e1 > pair_cap) e1 = (uint32_t)pair_cap;  // after an overflow (reported) rows stay in storage
     for (uint32_t e = e0; e < e1; ++e) {
         int b = (int)__ldg(&body_pairs[e].y);
+        float4 xb = __ldg(pos + b);
+        float bx = xb.x - xa.x, by = xb.y - xa.y, bz = xb.z - xa.z;
         int s = __ldg(pstart + b), m = __ldg(npart + b);
         for (int l = 0; l < m; ++l) {
-            float4 jp = __ldg(p_pos + s + l);
-            float dx = jp.x - ip.x, dy = jp.y - ip.y, dz = jp.z - ip.z;
+            float4 rj = __ldg(p_rel + s + l);
+            float dx = bx + (rj.x - ri.x), dy = by + (rj.y - ri.y), dz = bz + (rj.z - ri.z);
             float d2 = dx * dx + dy * dy + dz * dz;
-            float rr = ip.w + jp.w;
+            float rr = ri.w + rj.w;
             if (d2 < rr * rr && d2 > 0.f) {
                 float dist = sqrtf(d2);
                 float inv = 1.f / dist;
@@ -196,22 +223,28 @@ cudaError_t rb_integrate_cfg(float4* pos, float4* quat, float4* lin, const float
     if (n > 0) k_integrate_cfg<<<gr(n), 256, 0, st>>>(pos, quat, lin, ang, p, n);
     return cudaGetLastError();
 }
-cudaError_t rb_place_cfg(const float4* pos, const float4* quat, const float4* lin, const float4* ang,
-                         const int* shape, const int* pstart, const int* p_body, const float4* ref_pos,
-                         float4* p_pos, float4* p_vel, int np, cudaStream_t st) {
-    if (np > 0) k_place_cfg<<<gr(np), 256, 0, st>>>(pos, quat, lin, ang, shape, pstart, p_body, ref_pos, p_pos, p_vel, np);
+cudaError_t rb_place_cfg(const float4* quat, const float4* lin, const float4* ang, const int* shape,
+                         const int* pstart, const int* p_body, const float4* ref_pos, float4* p_rel, float4* p_vel,
+                         int np, cudaStream_t st) {
+    if (np > 0) k_place_cfg<<<gr(np), 256, 0, st>>>(quat, lin, ang, shape, pstart, p_body, ref_pos, p_rel, p_vel, np);
     return cudaGetLastError();
 }
-cudaError_t rb_body_aabb(const float4* p_pos, const int* pstart, const int* npart, float4* bmin, float4* bmax, int n,
-                         cudaStream_t st) {
-    if (n > 0) k_body_aabb<<<gr(n), 256, 0, st>>>(p_pos, pstart, npart, bmin, bmax, n);
+cudaError_t rb_abs_pos(const float4* pos, const int* p_body, const float4* p_rel, float4* p_pos, int np,
+                       cudaStream_t st) {
+    if (np > 0) k_abs_pos<<<gr(np), 256, 0, st>>>(pos, p_body, p_rel, p_pos, np);
     return cudaGetLastError();
 }
-cudaError_t rb_forces_cfg(const float4* p_pos, const float4* p_vel, const int* p_body, const int* pstart,
-                          const int* npart, const uint2* body_pairs, const uint32_t* rowoff, const CfgParams& p,
-                          float4* p_force, int np, cudaStream_t st) {
+cudaError_t rb_body_aabb(const float4* pos, const float4* p_rel, const int* pstart, const int* npart, float4* bmin,
+                         float4* bmax, int n, cudaStream_t st) {
+    if (n > 0) k_body_aabb<<<gr(n), 256, 0, st>>>(pos, p_rel, pstart, npart, bmin, bmax, n);
+    return cudaGetLastError();
+}
+cudaError_t rb_forces_cfg(const float4* pos, const float4* p_rel, const float4* p_vel, const int* p_body,
+                          const int* pstart, const int* npart, const uint2* body_pairs, const uint32_t* rowoff,
+                          uint64_t pair_cap, const CfgParams& p, float4* p_force, int np, cudaStream_t st) {
     if (np > 0)
-        k_forces_cfg<<<gr(np), 256, 0, st>>>(p_pos, p_vel, p_body, pstart, npart, body_pairs, rowoff, p, p_force, np);
+        k_forces_cfg<<<gr(np), 256, 0, st>>>(pos, p_rel, p_vel, p_body, pstart, npart, body_pairs, rowoff, pair_cap, p,
+                                             p_force, np);
     return cudaGetLastError();
 }
 cudaError_t rb_update_cfg(float4* lin, float4* ang, const float4* quat, const float* inv_mass, const int* shape,

@@ -173,12 +173,15 @@ __global__ void k_clear_force_ref(const float4* p_pos, const float4* p_vel, cons
 __global__ void k_pair_force_ref(const float4* p_pos, const float4* p_vel, const int2* pairs, const int* entries,
                                  int num_pairs, int num_entries, const unsigned long long* d_num_pairs2,
                                  const uint32_t* d_num_entries, const float* p_mass, float sp, float dp,
-                                 float4* p_force, float dt, int quirk) {
+                                 float4* p_force, float dt, int quirk, int pair_cap, int entry_cap) {
     int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (d_num_entries) num_entries = (int)*d_num_entries;
-    if (d_num_pairs2) num_pairs = (int)(2ull * *d_num_pairs2);
+    if (d_num_entries) num_entries = (int)min(*d_num_entries, (uint32_t)entry_cap);
+    if (d_num_pairs2) num_pairs = (int)min(2ull * *d_num_pairs2, (unsigned long long)pair_cap);
+    if (num_pairs > pair_cap) num_pairs = pair_cap;  // rows never leave the list's storage
     if (e >= num_entries) return;
     int b0 = entries[e], b1 = (e + 1 < num_entries) ? entries[e + 1] : num_pairs;
+    if (b1 > num_pairs) b1 = num_pairs;
+    if (b0 < 0 || b0 >= b1) return;
     int i = pairs[b0].x;
     float dt2i = 1.f / (dt * dt), dti = 1.f / dt;
     f4 ip = ld(p_pos + i), iv = ld(p_vel + i);
@@ -278,11 +281,11 @@ cudaError_t rb_clear_force_ref(const float4* p_pos, const float4* p_vel, const f
 cudaError_t rb_pair_force_ref(const float4* p_pos, const float4* p_vel, const int2* pairs, const int* entries,
                               int num_pairs, int num_entries, int max_entries, const unsigned long long* d_np2,
                               const uint32_t* d_ne, const float* p_mass, float sp, float dp, float4* p_force,
-                              float dt, int quirk, cudaStream_t st) {
+                              float dt, int quirk, int pair_cap, cudaStream_t st) {
     int g = d_ne ? max_entries : num_entries;
     if (g > 0)
         k_pair_force_ref<<<grid_for(g), 256, 0, st>>>(p_pos, p_vel, pairs, entries, num_pairs, num_entries, d_np2,
-                                                      d_ne, p_mass, sp, dp, p_force, dt, quirk);
+                                                      d_ne, p_mass, sp, dp, p_force, dt, quirk, pair_cap, g);
     return cudaGetLastError();
 }
 cudaError_t rb_update_velocity_ref(float4* lin, float4* ang, const float4* quat, const float* inv_mass,

@@ -1,46 +1,110 @@
-// FP64 scene statistics -> sweep axes and grid.  Host and device: the PCA
-// kernel runs it in its last CTA per scene, and the library exports a host
-// copy (gsap_debug_choose_scene) so the solver can be checked without a GPU.
+// Scene statistics -> sweep axes and grid.  Host and device: the PCA kernel
+// runs it in its last CTA per scene, and the library exports a host copy
+// (gsap_debug_scene_solve) so the solver can be checked without a GPU.
+//
+// FP64 where the result needs it: the covariance combine and the 3x3
+// symmetric eigensolve.  The solve runs a cyclic Jacobi in FP32 first (FP32
+// rotations are cheap on the GPU, FP64 ones are not) and then polishes in
+// FP64: B = V32^T C V32 is formed in FP64 and diagonalised by FP64 Jacobi
+// rotations until its off-diagonal part is below 1e-17 of its diagonal, which
+// takes one or two sweeps because B is already nearly diagonal.  The
+// eigenvectors are V32 W in FP64.  The grid choice that follows is a
+// heuristic (any grid gives the same pair set) and runs in FP32.
 #pragma once
 #include "internal.cuh"
 #include <math.h>
 
 namespace gsap {
 
-
-// Cyclic Jacobi for a symmetric 3x3 matrix (FP64).  On return a holds the
-// diagonalised matrix and v the eigenvectors as columns.
-__host__ __device__ inline void jacobi3(double a[3][3], double v[3][3]) {
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) v[i][j] = (i == j) ? 1.0 : 0.0;
-    const double scale = fabs(a[0][0]) + fabs(a[1][1]) + fabs(a[2][2]) + 1e-300;
-    for (int sweep = 0; sweep < 32; ++sweep) {
-        double off = fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]);
-        if (off <= 1e-17 * scale) break;
-        for (int p = 0; p < 2; ++p)
-            for (int q = p + 1; q < 3; ++q) {
-                double apq = a[p][q];
-                if (fabs(apq) <= 1e-300) continue;
-                double theta = (a[q][q] - a[p][p]) / (2.0 * apq);
-                double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-                double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
-                for (int k = 0; k < 3; ++k) {  // A <- A J
-                    double akp = a[k][p], akq = a[k][q];
-                    a[k][p] = c * akp - s * akq;
-                    a[k][q] = s * akp + c * akq;
-                }
-                for (int k = 0; k < 3; ++k) {  // A <- J^T A
-                    double apk = a[p][k], aqk = a[q][k];
-                    a[p][k] = c * apk - s * aqk;
-                    a[q][k] = s * apk + c * aqk;
-                }
-                for (int k = 0; k < 3; ++k) {
-                    double vkp = v[k][p], vkq = v[k][q];
-                    v[k][p] = c * vkp - s * vkq;
-                    v[k][q] = s * vkp + c * vkq;
-                }
-            }
+// One cyclic Jacobi sweep step on (p, q) of a symmetric 3x3 matrix; T is
+// float or double.  Rotation by (c, s) with t = tan of the angle that zeroes
+// a[p][q]; accumulates the rotation into the columns of v.
+template <class T>
+__host__ __device__ inline void jacobi_rotate(T a[3][3], T v[3][3], int p, int q) {
+    T apq = a[p][q];
+    if (apq == T(0)) return;
+    T diff = a[q][q] - a[p][p];
+    T t;
+    if (fabs(apq) < T(1e-6) * fabs(diff)) {
+        t = apq / diff;  // small angle: tan(phi) = apq / diff to O(phi^3)
+    } else {
+        T theta = diff / (T(2) * apq);
+        t = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + sqrt(theta * theta + T(1)));
     }
+    T c = T(1) / sqrt(t * t + T(1)), s = t * c;
+    for (int k = 0; k < 3; ++k) {  // A <- A J
+        T akp = a[k][p], akq = a[k][q];
+        a[k][p] = c * akp - s * akq;
+        a[k][q] = s * akp + c * akq;
+    }
+    for (int k = 0; k < 3; ++k) {  // A <- J^T A
+        T apk = a[p][k], aqk = a[q][k];
+        a[p][k] = c * apk - s * aqk;
+        a[q][k] = s * apk + c * aqk;
+    }
+    for (int k = 0; k < 3; ++k) {
+        T vkp = v[k][p], vkq = v[k][q];
+        v[k][p] = c * vkp - s * vkq;
+        v[k][q] = s * vkp + c * vkq;
+    }
+}
+
+template <class T>
+__host__ __device__ inline void jacobi_sweeps(T a[3][3], T v[3][3], T tol, int max_sweeps) {
+    const T scale = fabs(a[0][0]) + fabs(a[1][1]) + fabs(a[2][2]) + T(1e-30);
+    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+        T off = fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]);
+        if (off <= tol * scale) break;
+        jacobi_rotate(a, v, 0, 1);
+        jacobi_rotate(a, v, 0, 2);
+        jacobi_rotate(a, v, 1, 2);
+    }
+}
+
+// Symmetric 3x3 eigensolve, FP64 result.  a is overwritten with the
+// diagonalised matrix, v receives the eigenvectors as columns.
+__host__ __device__ inline void eig3(double a[3][3], double v[3][3]) {
+    float af[3][3], vf[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            af[i][j] = (float)a[i][j];
+            vf[i][j] = (i == j) ? 1.f : 0.f;
+        }
+    jacobi_sweeps<float>(af, vf, 1e-7f, 12);
+    // B = V32^T A V32 in FP64
+    double V[3][3], t[3][3], b[3][3];
+    // re-orthonormalise the FP32 basis in FP64 (Gram-Schmidt, third column
+    // by cross product) so that V^T A V is an exact similarity transform
+    {
+        double c0[3] = {vf[0][0], vf[1][0], vf[2][0]}, c1[3] = {vf[0][1], vf[1][1], vf[2][1]};
+        double l0 = 1.0 / sqrt(c0[0] * c0[0] + c0[1] * c0[1] + c0[2] * c0[2]);
+        for (int k = 0; k < 3; ++k) c0[k] *= l0;
+        double d = c0[0] * c1[0] + c0[1] * c1[1] + c0[2] * c1[2];
+        for (int k = 0; k < 3; ++k) c1[k] -= d * c0[k];
+        double l1 = 1.0 / sqrt(c1[0] * c1[0] + c1[1] * c1[1] + c1[2] * c1[2]);
+        for (int k = 0; k < 3; ++k) c1[k] *= l1;
+        double c2[3] = {c0[1] * c1[2] - c0[2] * c1[1], c0[2] * c1[0] - c0[0] * c1[2], c0[0] * c1[1] - c0[1] * c1[0]};
+        for (int k = 0; k < 3; ++k) {
+            V[k][0] = c0[k];
+            V[k][1] = c1[k];
+            V[k][2] = c2[k];
+        }
+    }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) t[i][j] = a[i][0] * V[0][j] + a[i][1] * V[1][j] + a[i][2] * V[2][j];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) b[i][j] = V[0][i] * t[0][j] + V[1][i] * t[1][j] + V[2][i] * t[2][j];
+    for (int i = 0; i < 3; ++i)
+        for (int j = i + 1; j < 3; ++j) b[j][i] = b[i][j] = 0.5 * (b[i][j] + b[j][i]);
+    double w[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) w[i][j] = (i == j) ? 1.0 : 0.0;
+    jacobi_sweeps<double>(b, w, 1e-17, 16);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            v[i][j] = V[i][0] * w[0][j] + V[i][1] * w[1][j] + V[i][2] * w[2][j];
+            a[i][j] = b[i][j];
+        }
 }
 
 // Sums (FP64) of one scene -> axes, statistics and sweep grid.
@@ -51,14 +115,15 @@ struct SceneSums {
 };
 
 __host__ __device__ inline void choose_scene(const SceneSums& z, const BpArgs& A, uint64_t entry_cap, uint32_t n_total,
-                             Scene& out) {
+                                             Scene& out) {
     const double n = z.n > 0 ? z.n : 1.0;
-    double md[3] = {z.sd[0] / n, z.sd[1] / n, z.sd[2] / n};
-    // covariance about the mean, from sums about the pilot
+    const double inv_n = 1.0 / n;
+    double md[3] = {z.sd[0] * inv_n, z.sd[1] * inv_n, z.sd[2] * inv_n};
+    // covariance about the mean, from sums about the pilot (FP64)
     double C[3][3];
     const int idx[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
     for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) C[i][j] = z.sdd[idx[i][j]] / n - md[i] * md[j];
+        for (int j = 0; j < 3; ++j) C[i][j] = z.sdd[idx[i][j]] * inv_n - md[i] * md[j];
     double mean[3] = {z.pilot[0] + md[0], z.pilot[1] + md[1], z.pilot[2] + md[2]};
 
     double U[3][3], lam[3];
@@ -78,7 +143,7 @@ __host__ __device__ inline void choose_scene(const SceneSums& z, const BpArgs& A
         double a[3][3], v[3][3];
         for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 3; ++j) a[i][j] = 0.5 * (C[i][j] + C[j][i]);
-        jacobi3(a, v);
+        eig3(a, v);
         int o[3] = {0, 1, 2};
         double ev[3] = {a[0][0], a[1][1], a[2][2]};
         // descending eigenvalues, stable on ties
@@ -106,74 +171,80 @@ __host__ __device__ inline void choose_scene(const SceneSums& z, const BpArgs& A
             out.u[3 * r + c] = (float)U[r][c];
         }
     }
-    // projected statistics on each axis (using the FP32 axes actually applied)
-    double mc[3], sig[3], hw[3], sw[3];
-    double mh[3] = {z.sh[0] / n, z.sh[1] / n, z.sh[2] / n};
+    // ---- grid choice: a heuristic, FP32 from here on
+    float Cf[3][3], meanf[3], shf[3], shhf[6];
+    for (int i = 0; i < 3; ++i) {
+        meanf[i] = (float)mean[i];
+        shf[i] = (float)z.sh[i];
+        for (int j = 0; j < 3; ++j) Cf[i][j] = (float)C[i][j];
+    }
+    for (int k = 0; k < 6; ++k) shhf[k] = (float)z.shh[k];
+    const float nf = (float)n, invf = 1.f / nf;
+    float mc[3], sig[3], hw[3], sw[3];
     for (int r = 0; r < 3; ++r) {
-        double u0 = out.u[3 * r], u1 = out.u[3 * r + 1], u2 = out.u[3 * r + 2];
-        mc[r] = u0 * mean[0] + u1 * mean[1] + u2 * mean[2];
-        double var = 0;
-        double uu[3] = {u0, u1, u2};
+        const float* u = &out.u[3 * r];
+        mc[r] = u[0] * meanf[0] + u[1] * meanf[1] + u[2] * meanf[2];
+        float var = 0.f;
         for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j) var += uu[i] * C[i][j] * uu[j];
-        sig[r] = sqrt(var > 0 ? var : 0);
-        hw[r] = fabs(u0) * mh[0] + fabs(u1) * mh[1] + fabs(u2) * mh[2];            // mean half width
-        sw[r] = 2.0 * (fabs(u0) * z.sh[0] + fabs(u1) * z.sh[1] + fabs(u2) * z.sh[2]);  // sum of widths
+            for (int j = 0; j < 3; ++j) var += u[i] * Cf[i][j] * u[j];
+        sig[r] = sqrtf(var > 0.f ? var : 0.f);
+        sw[r] = 2.f * (fabsf(u[0]) * shf[0] + fabsf(u[1]) * shf[1] + fabsf(u[2]) * shf[2]);  // sum of widths
+        hw[r] = 0.5f * sw[r] * invf;                                                           // mean half width
     }
     // lower-bound quantisation range along u1
-    double qr = 8.0 * sig[0] + 4.0 * hw[0];
-    if (!(qr > 1e-30)) qr = 1.0;
-    out.q_org = (float)(mc[0] - 4.0 * sig[0] - 2.0 * hw[0]);
-    out.q_range = (float)qr;
+    float qr = 8.f * sig[0] + 4.f * hw[0];
+    if (!(qr > 1e-30f) || !isfinite(qr)) qr = 1.f;
+    out.q_org = mc[0] - 4.f * sig[0] - 2.f * hw[0];
+    out.q_range = qr;
     // secondary-axis grid
-    double r2 = 8.0 * sig[1] + 2.0 * hw[1], r3 = 8.0 * sig[2] + 2.0 * hw[2];
-    if (!(r2 > 1e-30)) r2 = 1.0;
-    if (!(r3 > 1e-30)) r3 = 1.0;
-    double width = hw[1] + hw[2];  // mean full width averaged over the two axes
-    double cf = A.cell_factor > 0 ? A.cell_factor : 1.5;
-    double target = 16.0;          // aim for at least this many objects per cell
-    double s = cf * width;
-    double sd = sqrt(r2 * r3 * target / (z.n > 1 ? z.n : 1.0));
+    float r2 = 8.f * sig[1] + 2.f * hw[1], r3 = 8.f * sig[2] + 2.f * hw[2];
+    if (!(r2 > 1e-30f) || !isfinite(r2)) r2 = 1.f;
+    if (!(r3 > 1e-30f) || !isfinite(r3)) r3 = 1.f;
+    const float width = hw[1] + hw[2];  // mean full width averaged over the two axes
+    const float cf = A.cell_factor > 0 ? A.cell_factor : 1.5f;
+    const float target = 16.f;           // aim for at least this many objects per cell
+    float s = cf * width;
+    float sd = sqrtf(r2 * r3 * target / (nf > 1.f ? nf : 1.f));
     if (s < sd) s = sd;
-    if (!(s > 0)) s = 1.0;
+    if (!(s > 0.f) || !isfinite(s)) s = r2 > r3 ? r2 : r3;
     const int qmin = A.key_bits >= 32 ? 12 : 8;
-    double bmax = ldexp(1.0, (int)A.key_bits - qmin);
-    double bcap = floor(bmax * (z.n > 0 ? z.n : 1.0) / (n_total > 0 ? n_total : 1u));
-    if (bcap < 1) bcap = 1;
-    double ecap = floor((double)entry_cap * (z.n > 0 ? z.n : 1.0) / (n_total > 0 ? n_total : 1u));
+    const float bmax = ldexpf(1.f, (int)A.key_bits - qmin);
+    const float share = nf / (float)(n_total > 0 ? n_total : 1u);
+    float bcap = floorf(bmax * share);
+    if (bcap < 1.f) bcap = 1.f;
+    const float ecap = floorf((float)entry_cap * share);
     // sum over objects of w2*w3: 4 sum_{m,l} |u2m| |u3l| sum h_m h_l
     const int hidx[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
-    double sww = 0;
+    float sww = 0.f;
     for (int m = 0; m < 3; ++m)
-        for (int l = 0; l < 3; ++l)
-            sww += 4.0 * fabs((double)out.u[3 + m]) * fabs((double)out.u[6 + l]) * z.shh[hidx[m][l]];
-    double G2 = 1, G3 = 1;
+        for (int l = 0; l < 3; ++l) sww += 4.f * fabsf(out.u[3 + m]) * fabsf(out.u[6 + l]) * shhf[hidx[m][l]];
+    float G2 = 1.f, G3 = 1.f;
     for (int it = 0; it < 400; ++it) {
-        G2 = fmin(ceil(r2 / s), 65535.0);
-        G3 = fmin(ceil(r3 / s), 65535.0);
-        if (G2 < 1) G2 = 1;
-        if (G3 < 1) G3 = 1;
+        G2 = fminf(ceilf(r2 / s), 65535.f);
+        G3 = fminf(ceilf(r3 / s), 65535.f);
+        if (G2 < 1.f) G2 = 1.f;
+        if (G3 < 1.f) G3 = 1.f;
         bool ok = G2 * G3 <= bcap;
         if (ok) {
             // worst-case entries: per axis min(G, w*inv + 2) cells
-            double i2 = G2 / r2 * (1.0 + 1e-5), i3 = G3 / r3 * (1.0 + 1e-5);
-            double e;
-            if (G2 == 1 && G3 == 1) e = z.n;
-            else if (G2 == 1) e = sw[2] * i3 + 2.0 * z.n;
-            else if (G3 == 1) e = sw[1] * i2 + 2.0 * z.n;
-            else e = 4.0 * z.n + 2.0 * (sw[1] * i2 + sw[2] * i3) + sww * i2 * i3;
-            ok = e * 1.001 + 64.0 <= ecap;
+            float i2 = G2 / r2 * (1.f + 1e-4f), i3 = G3 / r3 * (1.f + 1e-4f);
+            float e;
+            if (G2 == 1.f && G3 == 1.f) e = nf;
+            else if (G2 == 1.f) e = sw[2] * i3 + 2.f * nf;
+            else if (G3 == 1.f) e = sw[1] * i2 + 2.f * nf;
+            else e = 4.f * nf + 2.f * (sw[1] * i2 + sw[2] * i3) + sww * i2 * i3;
+            ok = e * 1.01f + 64.f <= ecap;
         }
         if (ok) break;
-        s *= 1.1;
-        if (it == 399) { G2 = 1; G3 = 1; }
+        s *= 1.1f;
+        if (it == 399) { G2 = 1.f; G3 = 1.f; }
     }
     out.G2 = (uint32_t)G2;
     out.G3 = (uint32_t)G3;
-    out.c2_org = (float)(mc[1] - 4.0 * sig[1] - hw[1]);
-    out.c3_org = (float)(mc[2] - 4.0 * sig[2] - hw[2]);
-    out.c2_inv = (float)(G2 / r2);
-    out.c3_inv = (float)(G3 / r3);
+    out.c2_org = mc[1] - 4.f * sig[1] - hw[1];
+    out.c3_org = mc[2] - 4.f * sig[2] - hw[2];
+    out.c2_inv = G2 / r2;
+    out.c3_inv = G3 / r3;
     out.n = (uint32_t)z.n;
 }
 

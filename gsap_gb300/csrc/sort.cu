@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(BpScratch S, const uint32
                                                        const uint32_t* __restrict__ vin,
                                                        uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
                                                        const uint32_t* count_ptr, uint32_t cap, int pass,
-                                                       uint32_t spin) {
+                                                       uint32_t spin, SortGather G) {
     constexpr int TILE = kThreads * ITEMS;
     __shared__ uint32_t s_k[TILE];
     __shared__ uint32_t s_v[TILE];
@@ -133,8 +133,14 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(BpScratch S, const uint32
         for (uint32_t i = tid; i < tn; i += kThreads) {
             uint32_t kk = s_k[i];
             uint32_t g = s_gb[(kk >> shift) & 255u] + i;
+            uint32_t vv = s_v[i];
             kout[g] = kk;
-            vout[g] = s_v[i];
+            vout[g] = vv;
+            if (G.smin) {  // last pass of the broadphase: entries in sorted order
+                G.smin[g] = __ldg(G.mn + vv);
+                if (G.mx) G.smax[g] = __ldg(G.mx + vv);
+                G.scell[g] = __ldg(G.objcell + vv);
+            }
         }
         __syncthreads();
     }
@@ -184,8 +190,11 @@ cudaError_t launch_sort_prep(const BpScratch& s, const uint32_t* keys, const uin
 
 cudaError_t launch_sort_pass(const BpScratch& s, int pass, int passes, const uint32_t* kin, const uint32_t* vin,
                              uint32_t* kout, uint32_t* vout, const uint32_t* count_ptr, uint64_t cap,
-                             uint32_t spin, cudaStream_t st) {
+                             uint32_t spin, cudaStream_t st, const SortGather* gather) {
     (void)passes;
+    SortGather G;
+    if (gather) G = *gather;
+    else G = SortGather{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     static int grid = 0;
     if (grid == 0) {
         int per_sm = 0;
@@ -193,7 +202,7 @@ cudaError_t launch_sort_pass(const BpScratch& s, int pass, int passes, const uin
         grid = sm_count() * (per_sm > 0 ? per_sm : 1);
     }
     uint32_t c = cap > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)cap;
-    k_onesweep<kSortItems><<<grid, kThreads, 0, st>>>(s, kin, vin, kout, vout, count_ptr, c, pass, spin);
+    k_onesweep<kSortItems><<<grid, kThreads, 0, st>>>(s, kin, vin, kout, vout, count_ptr, c, pass, spin, G);
     return cudaGetLastError();
 }
 

@@ -13,14 +13,18 @@
 // while the candidate key is <= (bucket | q(hi1)): the q map is monotone, so
 // every later entry of the same cell whose interval on u1 can meet this one
 // is visited, and the scan stops at the cell (and scene) boundary by
-// construction.  Candidates pass the exact test on the original FP32 bounds
-// (closed AABB test of Aabb::overlaps, include/aabb.h:47-57, or the strict
-// squared sphere test of SapKernel.cu:1897-1903 with one rounding per
-// operation) and the owner-cell rule: a pair is reported only in the cell
-// holding max(lo2_i, lo2_j), max(lo3_i, lo3_j), which both objects touch, so
-// each overlapping pair comes out exactly once and no sort + unique pass is
+// construction.  The last sort pass wrote every entry's bounds and
+// lower-corner cell in sorted order, so lane L at step k reads entry
+// e + L + k: the 32 lanes read one contiguous run and the next step re-reads
+// it shifted by one (L1 hits) -- no random gathers in the hot loop.
+// Candidates pass the exact test on the original FP32 bounds (closed AABB
+// test of Aabb::overlaps, include/aabb.h:47-57, or the strict squared
+// sphere test of SapKernel.cu:1897-1903 with one rounding per operation)
+// and the owner-cell rule: a pair is reported only in the cell holding
+// (max(lo2_i, lo2_j), max(lo3_i, lo3_j)), which both objects touch, so each
+// overlapping pair comes out exactly once and no sort + unique pass is
 // needed.  Hits are compacted through a per-warp shared-memory buffer that
-// reserves global space with one atomic per 128 pairs.
+// reserves global space with one atomic per up to 128 pairs.
 #include "internal.cuh"
 
 namespace gsap {
@@ -42,11 +46,15 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const uint32_t lt = lanemask_lt();
     Ctrl* C = S.ctrl;
+    const float4* __restrict__ smin = S.smin;
+    const float4* __restrict__ smax = S.smax;
+    const uint32_t* __restrict__ scell = S.scell;
     const uint32_t E = (uint32_t)min((uint64_t)C->entry_count, S.entry_cap);
     const uint32_t Q = C->qbits;
     const uint32_t qmask = (1u << Q) - 1u;
     const float qmax = (float)qmask;
     uint32_t nbuf = 0;
+    unsigned long long tests = 0;
 
     auto flush = [&]() {
         __syncwarp();
@@ -81,10 +89,10 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
             i = vals[e];
             const uint32_t s = S.objscene ? S.objscene[i] : 0u;
             const Scene* sc = &S.scenes[s];
-            pa = A.mn[i];
+            pa = smin[e];
             float3 a, b;
             if (MODE == 0) {
-                pb = A.mx[i];
+                pb = smax[e];
                 a = make_float3(pa.x, pa.y, pa.z);
                 b = make_float3(pb.x, pb.y, pb.z);
             } else {
@@ -102,22 +110,23 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
             uint32_t G3 = sc->G3;
             c2 = local / G3;
             c3 = local - c2 * G3;
-            ci = S.objcell[i];
+            ci = scell[e];
         }
         uint32_t j = e + 1;
         while (true) {
             bool act = live && j < E;
             if (act) act = __ldg(keys + j) <= kb;
             live = act;
-            if (!__any_sync(0xffffffffu, act)) break;
+            const uint32_t am = __ballot_sync(0xffffffffu, act);
+            if (!am) break;
+            tests += __popc(am);
             bool hit = false;
             uint32_t o = 0;
             if (act) {
-                o = __ldg(vals + j);
-                float4 qa = __ldg(A.mn + o);
+                float4 qa = __ldg(smin + j);
                 bool ov;
                 if (MODE == 0) {
-                    float4 qb = __ldg(A.mx + o);
+                    float4 qb = __ldg(smax + j);
                     ov = pa.x <= qb.x && qa.x <= pb.x && pa.y <= qb.y && qa.y <= pb.y && pa.z <= qb.z &&
                          qa.z <= pb.z;
                 } else {
@@ -127,8 +136,11 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
                     ov = t1 < __fmul_rn(r, r);
                 }
                 if (ov) {
-                    uint32_t co = __ldg(S.objcell + o);
-                    hit = max(ci >> 16, co >> 16) == c2 && max(ci & 0xFFFFu, co & 0xFFFFu) == c3;
+                    uint32_t co = __ldg(scell + j);
+                    if (max(ci >> 16, co >> 16) == c2 && max(ci & 0xFFFFu, co & 0xFFFFu) == c3) {
+                        hit = true;
+                        o = __ldg(vals + j);
+                    }
                 }
             }
             uint32_t hm = __ballot_sync(0xffffffffu, hit);
@@ -142,6 +154,7 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
         }
     }
     flush();
+    if (lane == 0 && tests) atomicAdd(&C->tests, tests);
 }
 
 cudaError_t launch_sweep(const BpScratch& s, const BpArgs& a, const uint32_t* keys, const uint32_t* vals,

@@ -19,6 +19,12 @@ int gsap_debug_scene_solve(const double* sums18, const double* hmax3, const doub
                            uint32_t n_total, uint32_t axis_mode, float cell_factor, uint32_t key_bits,
                            uint64_t entry_cap, double* out17);
 
+/* Counters of the last broadphase call of a handle (synchronizes):
+ * out8 = sweep entries, candidate tests, pairs, buckets, q bits, long rows
+ * of the canonical sort, key bits, device error word.  Returns 0. */
+struct gsap_sap;
+int gsap_debug_stats(struct gsap_sap* h, uint64_t* out8, void* stream);
+
 /* Sizes of internal device structures (control block, scene record, PCA
  * partial, sort tile) for layout checks.  Returns 0. */
 int gsap_debug_sizes(uint32_t* out4);

@@ -55,12 +55,16 @@ def lib():
         L.orc_bf_sphere.restype = C.c_int64
         L.orc_sap_ref.argtypes = [C.c_int, P, P, C.c_uint32, P, C.c_int64, C.c_int]
         L.orc_sap_ref.restype = C.c_int64
+        L.orc_sap_ref_sampled.argtypes = [C.c_int, P, P, C.c_uint32, C.c_uint32, P, C.c_int64, C.c_int]
+        L.orc_sap_ref_sampled.restype = C.c_int64
         L.orc_both_directions.argtypes = [P, C.c_int64, P, P]
         L.orc_both_directions.restype = C.c_int64
         L.orc_radix_sort_u32.argtypes = [P, P, C.c_uint32, C.c_int]
         L.orc_radix_sort_u32.restype = None
         L.orc_float_flip.argtypes = [C.c_float]
         L.orc_float_flip.restype = C.c_uint32
+        L.orc_normalize_quats.argtypes = [P, C.c_int]
+        L.orc_normalize_quats.restype = None
         L.orc_rb_step_ref.argtypes = [P, P, C.c_int64, C.c_int]
         L.orc_rb_step_ref.restype = C.c_int64
         L.orc_rb_step_cfg_f64.argtypes = [P, P, C.c_int]
@@ -128,6 +132,15 @@ def sap_ref(mode, mn, mx=None, threads=0):
                       _ptr(mn), _ptr(mx))
 
 
+def sap_ref_sampled(mode, mn, mx, stride, threads=0):
+    """orc_sap_ref with the sweep started from every stride-th object only."""
+    mn = _f4(mn)
+    mx = _f4(mx) if mx is not None else None
+    L = lib()
+    return _run_pairs(lambda a, b, p, c: L.orc_sap_ref_sampled(mode, a, b, C.c_uint32(len(mn)), C.c_uint32(stride),
+                                                               p, c, threads), _ptr(mn), _ptr(mx))
+
+
 def both_directions(pairs):
     """Reference output format: both-direction int2 list and pairEntries."""
     pairs = np.ascontiguousarray(pairs, dtype=np.uint32)
@@ -189,6 +202,13 @@ class RbStateF64(C.Structure):
         (name, C.c_void_p) for name in (
             "pos", "quat", "lin_vel", "ang_vel", "shape_idx", "p_start", "n_part", "scene",
             "inv_mass", "ref_pos", "shape_inv_inertia", "p_pos", "p_vel", "p_force")]
+
+
+def normalize_quats(q):
+    """setRbData's upload normalisation, in place on an (n, 4) float32 array."""
+    assert q.dtype == np.float32 and q.flags.c_contiguous
+    lib().orc_normalize_quats(_ptr(q), len(q))
+    return q
 
 
 def rb_step_ref(state: dict, dt, sp_multip, dp_multip, max_lin_vel=0.0, gravity_y=-5.0,

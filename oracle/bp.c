@@ -168,7 +168,7 @@ static void pv_push(pvec* v, uint64_t x) {
  * radixsort.cu), then scan forward while lo_j <= hi_i
  * (SapKernel.cu:1880-1913: break once d_pos[cur] > d_pos[i] + 2r). */
 static void sweep_group(int mode, const float* mn, const float* mx, int ax,
-                        uint32_t* ids, uint32_t m, pvec* out, int nt) {
+                        uint32_t* ids, uint32_t m, pvec* out, int nt, uint32_t stride) {
     if (m < 2) return;
     uint32_t* keys = (uint32_t*)malloc((size_t)m * 4);
     float* lo = (float*)malloc((size_t)m * 4);
@@ -202,8 +202,8 @@ static void sweep_group(int mode, const float* mn, const float* mx, int ax,
 #pragma omp parallel num_threads(nt)
     {
         pvec local = {0, 0, 0};
-#pragma omp for schedule(dynamic, 256)
-        for (int64_t a = 0; a < (int64_t)m; ++a) {
+#pragma omp for schedule(dynamic, 64)
+        for (int64_t a = 0; a < (int64_t)m; a += stride) {
             uint32_t i = ids[a];
             float h = hi[a];
             for (uint32_t b = (uint32_t)a + 1; b < m && lo[b] <= h; ++b) {
@@ -228,7 +228,13 @@ static void sweep_group(int mode, const float* mn, const float* mx, int ax,
 
 int64_t orc_sap_ref(int mode, const float* mn, const float* mx, uint32_t n,
                     uint32_t* pairs, int64_t cap, int threads) {
+    return orc_sap_ref_sampled(mode, mn, mx, n, 1, pairs, cap, threads);
+}
+
+int64_t orc_sap_ref_sampled(int mode, const float* mn, const float* mx, uint32_t n, uint32_t stride,
+                            uint32_t* pairs, int64_t cap, int threads) {
     if (n < 2) return 0;
+    if (stride == 0) stride = 1;
     int nt = nthreads(threads);
     /* centres: sphere xyz, or AABB midpoints */
     double mean[3] = {0, 0, 0}, var[3] = {0, 0, 0};
@@ -265,7 +271,7 @@ int64_t orc_sap_ref(int mode, const float* mn, const float* mx, uint32_t n,
         grp[q][gn[q]++] = i;
     }
     pvec all = {0, 0, 0};
-    for (int q = 0; q < 4; ++q) sweep_group(mode, mn, mx, axis, grp[q], gn[q], &all, nt);
+    for (int q = 0; q < 4; ++q) sweep_group(mode, mn, mx, axis, grp[q], gn[q], &all, nt, stride);
 
     /* Cross pass (cullCrossSphereMultiple :557-635, cullRelevantSphereMultiple
      * :968-1059): maxR over objects straddling a plane, then every object
@@ -300,11 +306,11 @@ int64_t orc_sap_ref(int mode, const float* mn, const float* mx, uint32_t n,
         }
         if ((h1 >= -maxR && l1 <= maxR) || (h2 >= -maxR && l2 <= maxR)) grp[0][rn++] = i;
     }
-    if (rn > 0 && rn < n) sweep_group(mode, mn, mx, axis, grp[0], rn, &all, nt);
+    if (rn > 0 && rn < n) sweep_group(mode, mn, mx, axis, grp[0], rn, &all, nt, stride);
     else if (rn == n) { /* every object is relevant: the quadrant sweeps are
                            not enough, sweep them all together */
         for (uint32_t i = 0; i < n; ++i) grp[0][i] = i;
-        sweep_group(mode, mn, mx, axis, grp[0], n, &all, nt);
+        sweep_group(mode, mn, mx, axis, grp[0], n, &all, nt, stride);
     }
 
     /* Canonicalise: sort + unique (Sap.cpp:269-291, cullIndex :2249-2265). */

@@ -48,6 +48,13 @@ int64_t orc_bf_sphere(const float* spheres, uint32_t n,
 int64_t orc_sap_ref(int mode, const float* mn, const float* mx, uint32_t n,
                     uint32_t* pairs, int64_t cap, int threads);
 
+/* Same, with the sweep started only from every stride-th sorted object of
+ * each group (axis choice, sorts, partition and canonicalisation stay
+ * full-size): a bounded sample of the reference algorithm's work at the
+ * full scene's density, for timing.  stride = 1 is orc_sap_ref. */
+int64_t orc_sap_ref_sampled(int mode, const float* mn, const float* mx, uint32_t n, uint32_t stride,
+                            uint32_t* pairs, int64_t cap, int threads);
+
 /* The reference's output format (SapKernel.cu:2249-2360, Sap.cpp:326-329)
  * from a sorted unique (i<j) list: both directions (i,j) and (j,i) sorted by
  * (first, second), zero-based int2, plus pairEntries[k] = index of the first
@@ -107,6 +114,10 @@ typedef struct orc_ref_params {
     int torque_quirk;  /* 1 = angVel += tau*dt (reference, :260-261); 0 = I^-1 tau dt */
     int pair_loop_quirk; /* 1 = stop a row after pair index numPairEntries (:201) */
 } orc_ref_params;
+
+/* Upload normalisation of setRbData (ParticleRigidBody.cpp:82-86):
+ * q *= 1 / sqrtf(dot4(q, q)) for n float4 quaternions (quaternion.h:116-128). */
+void orc_normalize_quats(float* quat, int n);
 
 /* Reference-order FP32 step.  Uses a brute-force sphere pair list built
  * internally (pair capacity max_pairs).  Returns the number of

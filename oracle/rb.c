@@ -70,6 +70,10 @@ static inline void spring_coeff(float imi, float jmi, float dt2i, float dti, flo
     *d = m * dti * (1.f - dp);
 }
 
+void orc_normalize_quats(float* quat, int n) {
+    for (int i = 0; i < n; ++i) st4(quat + 4 * i, divs(ld4(quat + 4 * i), len4(ld4(quat + 4 * i))));
+}
+
 int64_t orc_rb_step_ref(orc_rb_state* s, const orc_ref_params* p, int64_t max_pairs, int threads) {
     const float dt = p->dt;
     const int nb = s->n_bodies;

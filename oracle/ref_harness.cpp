@@ -66,6 +66,12 @@ int64_t ref_bf_aabb(const float* mn, const float* mx, uint32_t n, uint32_t* pair
     return np;
 }
 
+/* The upload normalisation of setRbData (ParticleRigidBody.cpp:82-86):
+ * Quaternion::normalizeQ on every body quaternion. */
+void ref_normalize_quats(float4* quat, int n) {
+    for (int i = 0; i < n; ++i) ((Quaternion*)quat)[i].normalizeQ();
+}
+
 void ref_integrate(float4* pos, float4* quat, float4* linVel, float4* angVel, float dt, int n) {
     launch(n, [&] { integrateK(pos, (Quaternion*)quat, linVel, angVel, dt, n); });
 }

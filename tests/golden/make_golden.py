@@ -135,8 +135,7 @@ def rb_scene(rng):
     pos[:, 0] = ((i % nrow) - nrow / 2) * spacing
     pos[:, 2] = (((i // nrow) % nrow) - nrow / 2) * spacing
     pos[:, 1] = (i // (nrow * nrow) + 1) * spacing * 0.5
-    quat = rng.uniform(-1, 1, (nb, 4)).astype(np.float32)
-    quat /= np.linalg.norm(quat, axis=1, keepdims=True).astype(np.float32)
+    quat = rng.uniform(-1, 1, (nb, 4)).astype(np.float32)  # raw: normalised at upload
     ang = rng.uniform(-5, 5, (nb, 4)).astype(np.float32)
     lin = np.zeros((nb, 4), np.float32)
     lin[:, :3] = rng.uniform(-1, 1, (nb, 3))
@@ -181,12 +180,14 @@ def ref_step(R, s, dt, spM, dpM, max_vel):
 
 def make_rb(rng, out):
     R = oracle.ref_lib()
-    for name in ("ref_integrate", "ref_update_particle_data", "ref_prepare", "ref_clear_force", "ref_pair_force",
+    for name in ("ref_normalize_quats", "ref_integrate", "ref_update_particle_data", "ref_prepare", "ref_clear_force", "ref_pair_force",
                  "ref_update_velocity"):
         getattr(R, name).restype = None
     s = rb_scene(rng)
     dt, spM, dpM, max_vel = 0.025, 2.1, 0.8, 0.25 / 0.01
-    data = {f"init__{k}": v.copy() for k, v in s.items()}
+    data = {f"init__{k}": v.copy() for k, v in s.items()}  # quaternions as uploaded (raw)
+    R.ref_normalize_quats.restype = None
+    R.ref_normalize_quats(s["quat"].ctypes.data_as(C.c_void_p), len(s["quat"]))  # setRbData
     for step in range(3):
         npairs, nent = ref_step(R, s, dt, spM, dpM, max_vel)
         for k in ("pos", "quat", "lin_vel", "ang_vel", "p_pos", "p_vel", "p_force", "inv_inertia"):

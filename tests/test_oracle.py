@@ -48,6 +48,7 @@ def test_rb_reference_step_matches_reference_kernels(oracle_lib):
     g = load("rb_ref_step_golden.npz")
     dt, spM, dpM, vmax, gy = (float(x) for x in g["params"])
     s = {k[len("init__"):]: g[k].copy() for k in g.files if k.startswith("init__")}
+    oracle_lib.normalize_quats(s["quat"])  # setRbData's upload normalisation
     for step in range(3):
         npairs = oracle_lib.rb_step_ref(s, dt, spM, dpM, max_lin_vel=vmax, gravity_y=gy, floor_clamp=True,
                                         torque_quirk=True, pair_loop_quirk=True)
