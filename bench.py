@@ -169,7 +169,7 @@ def run_ours(args, world, rank, local):
     n = args.n
     host_sets, R = make_inputs(rank, n, args.jitter_sets)
     dsets = [(torch.from_numpy(mn).to(dev), torch.from_numpy(mx).to(dev)) for mn, mx in host_sets]
-    sap = Sap(n)
+    sap = Sap(n, cell_factor=args.cell_factor, sort_bits=args.sort_bits)
     cap = 16 * n
     pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
     d_count = torch.zeros(1, dtype=torch.int64, device=dev)
@@ -302,7 +302,8 @@ def run_ours(args, world, rank, local):
                               "frac": round(pipe_gbs / peak, 4), "formula": "156 n + 8 P"},
         "stage_ms": {k: round(v, 4) for k, v in st_ms.items()},
         "sweep_stats": {"entries": stats["entries"], "tests": stats["tests"], "buckets": stats["buckets"],
-                        "qbits": stats["qbits"], "key_bits": stats["key_bits"]},
+                        "qbits": stats["qbits"], "warp_iters": stats["iters"],
+                        "lane_efficiency": round(stats["tests"] / max(1, 32 * stats["iters"]), 3)},
         "unsorted_ms_per_step": round(unsorted_ms, 4),
         "e2e": {"value": round(e2e_val, 3), "unit": "Mobjects/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": int(np.mean(d2h))},
@@ -466,6 +467,8 @@ def main():
     ap.add_argument("--bodies", type=int, default=65536)
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cell-factor", type=float, default=1.5, help="sweep cell size / mean projected width")
+    ap.add_argument("--sort-bits", type=int, default=32, choices=[24, 32])
     ap.add_argument("--jitter-sets", type=int, default=N_JITTER,
                     help="distinct jittered inputs cycled by the timed calls (64 = the workload)")
     args = ap.parse_args()

@@ -151,7 +151,7 @@ extern "C" gsap_sap* gsap_sap_create(uint32_t max_n, const gsap_config* cfg) {
     s.entry_cap = ecap;
     s.pair_cap_internal = (uint64_t)c.pair_factor * max_n + 4096;
     uint64_t tiles = (ecap + kSortTile - 1) / kSortTile + 1;
-    s.status_words = tiles * 256 + (max_n / 2048 + 2);
+    s.status_words = tiles * 256 + (max_n / 2048 + 2);  // digit words, scan words
     bool ok = true;
     auto A = [&](void** p, size_t bytes) {
         if (!ok) return;
@@ -254,7 +254,7 @@ static gsap_status record(gsap_sap* h, const Call& c, cudaStream_t st, bool time
     SortGather gather{c.mn, c.mode == GSAP_MODE_AABB ? c.mx : nullptr, s.objcell, s.smin, s.smax, s.scell};
     for (int p = 0; p < passes; ++p) {
         CK(launch_sort_pass(s, p, passes, s.keys[src], s.vals[src], s.keys[src ^ 1], s.vals[src ^ 1], count,
-                            s.entry_cap, a.spin_limit, st, p == passes - 1 ? &gather : nullptr));
+                            s.entry_cap, a.spin_limit, st, p == passes - 1 ? &gather : nullptr, true));
         src ^= 1;
     }
     mark();
@@ -333,6 +333,7 @@ static gsap_status finish(gsap_sap* h, cudaStream_t st, uint64_t* count_out, uin
         if (err & kErrEntryCap) return fail(GSAP_ERR_CAPACITY, "sweep entries exceeded the handle's capacity (raise entry_factor)");
         if (err & kErrCellRange) return fail(GSAP_ERR_CAPACITY, "too many sweep cells for the key width");
         if (err & kErrPairCap) return fail(GSAP_ERR_CAPACITY, "pairs exceeded an output capacity");
+        if (err & kErrInternal) return fail(GSAP_ERR_CUDA, "internal consistency check failed (device error word 0x%x)", err);
         return fail(GSAP_ERR_CUDA, "device error word 0x%x", err);
     }
     if (cnt > cap) return fail(GSAP_ERR_CAPACITY, "%llu pairs exceed the capacity %llu", (unsigned long long)cnt, (unsigned long long)cap);
@@ -539,7 +540,7 @@ extern "C" int gsap_debug_stats(gsap_sap* h, uint64_t* out8, void* stream) {
     out8[3] = c.total_buckets;
     out8[4] = c.qbits;
     out8[5] = c.long_rows;
-    out8[6] = c.key_bits;
+    out8[6] = c.iters;
     out8[7] = c.error;
     return 0;
 }

@@ -66,11 +66,11 @@ __global__ void __launch_bounds__(kThreads) k_scan(BpScratch S, const uint32_t* 
         }
         if (tid == 0) {
             uint64_t* st = S.status + t;
-            st_release_u64(st, lb_word(tag, t == 0 ? kFlagPrefix : kFlagAgg, tot));
+            st_lb_u64(st, lb_word(tag, t == 0 ? kFlagPrefix : kFlagAgg, tot));
             uint32_t ex = 0;
             if (t > 0) {
                 ex = lookback(S.status, t, 0, 1, tag, spin, &C->error);
-                st_release_u64(st, lb_word(tag, kFlagPrefix, ex + tot));
+                st_lb_u64(st, lb_word(tag, kFlagPrefix, ex + tot));
             }
             s_excl = ex;
             if (t == ntiles - 1) {
@@ -94,19 +94,42 @@ __global__ void __launch_bounds__(kThreads) k_scan(BpScratch S, const uint32_t* 
 }
 
 // Scatter pairs into their rows.  both: row i gets (i, j) and row j (j, i).
+// Each thread takes 4 pairs and issues their returning atomics back to back,
+// so the grid keeps many of them in flight instead of chaining one per
+// thread.
+constexpr int kScatterPer = 4;
 __global__ void __launch_bounds__(kThreads) k_scatter(BpScratch S, const uint2* __restrict__ in, uint64_t in_cap,
                                                       uint2* out, uint64_t out_cap, int both) {
     const uint64_t P = min((uint64_t)S.ctrl->pair_count, in_cap);
     const uint32_t* off = S.rowoff;
-    for (uint64_t k = (uint64_t)blockIdx.x * kThreads + threadIdx.x; k < P; k += (uint64_t)gridDim.x * kThreads) {
-        uint2 p = in[k];
-        uint64_t s = (uint64_t)off[p.x] + atomicSub(&S.rowcnt[p.x], 1u) - 1u;
-        if (s < out_cap) out[s] = p;
-        else atomicOr(&S.ctrl->error, kErrPairCap);
+    const uint64_t stride = (uint64_t)gridDim.x * kThreads;
+    for (uint64_t k0 = (uint64_t)blockIdx.x * kThreads + threadIdx.x; k0 < P; k0 += stride * kScatterPer) {
+        uint2 p[kScatterPer];
+        uint32_t a[kScatterPer], b[kScatterPer];
+#pragma unroll
+        for (int u = 0; u < kScatterPer; ++u) {
+            uint64_t k = k0 + u * stride;
+            p[u] = k < P ? in[k] : make_uint2(0xFFFFFFFFu, 0xFFFFFFFFu);
+        }
+#pragma unroll
+        for (int u = 0; u < kScatterPer; ++u)
+            if (p[u].x != 0xFFFFFFFFu) a[u] = atomicSub(&S.rowcnt[p[u].x], 1u);
         if (both) {
-            uint64_t s2 = (uint64_t)off[p.y] + atomicSub(&S.rowcnt[p.y], 1u) - 1u;
-            if (s2 < out_cap) out[s2] = make_uint2(p.y, p.x);
+#pragma unroll
+            for (int u = 0; u < kScatterPer; ++u)
+                if (p[u].x != 0xFFFFFFFFu) b[u] = atomicSub(&S.rowcnt[p[u].y], 1u);
+        }
+#pragma unroll
+        for (int u = 0; u < kScatterPer; ++u) {
+            if (p[u].x == 0xFFFFFFFFu) continue;
+            uint64_t s = (uint64_t)off[p[u].x] + a[u] - 1u;
+            if (s < out_cap) out[s] = p[u];
             else atomicOr(&S.ctrl->error, kErrPairCap);
+            if (both) {
+                uint64_t s2 = (uint64_t)off[p[u].y] + b[u] - 1u;
+                if (s2 < out_cap) out[s2] = make_uint2(p[u].y, p[u].x);
+                else atomicOr(&S.ctrl->error, kErrPairCap);
+            }
         }
     }
 }
@@ -159,14 +182,18 @@ __global__ void __launch_bounds__(kThreads) k_rowsort(BpScratch S, uint2* out, u
     }
 }
 
-constexpr int kLongRow = 4096;
+constexpr int kLongRow = 1024;  // per-warp shared-memory sort limit
 
-// One CTA per long row: bitonic sort in shared memory (rows up to 4096
-// pairs), odd-even transposition in place beyond that.
+// One warp per long row (rows of 33..1024 pairs; ~1% of rows at the 1M
+// workload): bitonic sort in the warp's slice of shared memory.  Longer rows
+// (pathological overlap) use an in-place odd-even transposition by the warp.
 __global__ void __launch_bounds__(kThreads) k_rowsort_long(BpScratch S, uint2* out, uint64_t out_cap) {
-    __shared__ uint32_t s[kLongRow];
+    __shared__ uint32_t s_all[kThreads / 32][kLongRow];
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t* s = s_all[wid];
     const uint32_t nlong = S.ctrl->long_rows;
-    for (uint32_t q = blockIdx.x; q < nlong; q += gridDim.x) {
+    const uint32_t warps = gridDim.x * (kThreads / 32);
+    for (uint32_t q = blockIdx.x * (kThreads / 32) + wid; q < nlong; q += warps) {
         const uint32_t r = S.longrows[q];
         uint64_t b = S.rowoff[r], e = S.rowoff[r + 1];
         if (e > out_cap) e = out_cap;
@@ -175,31 +202,31 @@ __global__ void __launch_bounds__(kThreads) k_rowsort_long(BpScratch S, uint2* o
         if (len <= (uint32_t)kLongRow) {
             uint32_t P = 32;
             while (P < len) P <<= 1;
-            for (uint32_t k = threadIdx.x; k < P; k += kThreads) s[k] = k < len ? out[b + k].y : 0xFFFFFFFFu;
-            __syncthreads();
+            for (uint32_t k = lane; k < P; k += 32) s[k] = k < len ? out[b + k].y : 0xFFFFFFFFu;
+            __syncwarp();
             for (uint32_t k = 2; k <= P; k <<= 1)
                 for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-                    for (uint32_t i = threadIdx.x; i < P; i += kThreads) {
-                        uint32_t l = i ^ j;
+                    for (uint32_t i = lane; i < P; i += 32) {
+                        const uint32_t l = i ^ j;
                         if (l > i) {
-                            bool up = (i & k) == 0;
-                            uint32_t a = s[i], c = s[l];
+                            const bool up = (i & k) == 0;
+                            const uint32_t a = s[i], c = s[l];
                             if (up ? (a > c) : (a < c)) { s[i] = c; s[l] = a; }
                         }
                     }
-                    __syncthreads();
+                    __syncwarp();
                 }
-            for (uint32_t k = threadIdx.x; k < len; k += kThreads) out[b + k].y = s[k];
+            for (uint32_t k = lane; k < len; k += 32) out[b + k].y = s[k];
+            __syncwarp();
         } else {
             for (uint32_t phase = 0; phase < len; ++phase) {
-                for (uint32_t i = 2 * threadIdx.x + (phase & 1); i + 1 < len; i += 2 * kThreads) {
-                    uint32_t a = out[b + i].y, c = out[b + i + 1].y;
+                for (uint32_t i = 2 * lane + (phase & 1); i + 1 < len; i += 64) {
+                    const uint32_t a = out[b + i].y, c = out[b + i + 1].y;
                     if (a > c) { out[b + i].y = c; out[b + i + 1].y = a; }
                 }
-                __syncthreads();
+                __syncwarp();
             }
         }
-        __syncthreads();
     }
 }
 
@@ -208,7 +235,7 @@ cudaError_t launch_canonical(const BpScratch& s, uint32_t n, const uint2* in_pai
                              uint32_t spin, cudaStream_t st) {
     const int grid = sm_count() * 4;
     k_scan<0><<<grid, kThreads, 0, st>>>(s, s.rowcnt, s.rowoff, nullptr, 0, n, 5, spin);
-    k_scatter<<<grid * 2, kThreads, 0, st>>>(s, in_pairs, in_cap, out_pairs, out_cap, both);
+    k_scatter<<<sm_count() * 32, kThreads, 0, st>>>(s, in_pairs, in_cap, out_pairs, out_cap, both);
     k_rowsort<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(s, out_pairs, out_cap, n);
     k_rowsort_long<<<sm_count() * 2, kThreads, 0, st>>>(s, out_pairs, out_cap);
     if (both && entries) k_scan<1><<<grid, kThreads, 0, st>>>(s, s.rowoff, nullptr, entries, entry_cap, n, 6, spin);

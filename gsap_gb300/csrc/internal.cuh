@@ -19,6 +19,7 @@ enum : uint32_t {
     kErrTimeout = 4u,      // a bounded wait gave up
     kErrNonFinite = 8u,    // NaN / Inf in the input bounds
     kErrCellRange = 16u,   // internal: grid wider than 65535 cells per axis
+    kErrInternal = 32u,    // an internal consistency check failed (index out of range)
 };
 
 // Look-back status word: [63:32] tag, [31:30] flag, [29:0] value.
@@ -46,6 +47,7 @@ struct Ctrl {
     uint32_t sort_n;          // key count of a standalone sort
     uint32_t long_rows;       // canonical output: rows longer than the register sort
     unsigned long long tests; // sweep: candidate pairs tested (diagnostics)
+    unsigned long long iters; // sweep: warp iterations of the candidate loop (diagnostics)
     uint32_t hist[kMaxPasses][256];
 };
 
@@ -58,7 +60,8 @@ struct Scene {
     uint32_t G2, G3;      // cells per secondary axis
     uint32_t bucket_base; // first global bucket id of this scene
     uint32_t n;           // objects in the scene
-    uint32_t pad[2];
+    float q_scale;        // 2^Q / q_range, set once Q is known (same value in every kernel)
+    uint32_t pad;
     double eig[3];        // eigenvalues, descending
     double mean[3];       // centre mean
     double axes[9];       // FP64 axes (rows)
@@ -86,7 +89,7 @@ struct BpScratch {
     uint32_t* objscene;        // per object scene id (batched only)
     uint32_t* keys[2];
     uint32_t* vals[2];
-    uint64_t* status;          // look-back words
+    uint64_t* status;          // look-back words (per tile and digit)
     float4* smin;              // sweep entries in sorted order: bounds (sphere in smin)
     float4* smax;
     uint32_t* scell;           // sorted entries: (c2lo << 16) | c3lo of the object
@@ -134,7 +137,7 @@ struct SortGather {
 cudaError_t launch_sort_pass(const BpScratch& s, int pass, int passes, const uint32_t* kin,
                              const uint32_t* vin, uint32_t* kout, uint32_t* vout,
                              const uint32_t* count_ptr, uint64_t cap, uint32_t spin, cudaStream_t st,
-                             const SortGather* gather = nullptr);
+                             const SortGather* gather = nullptr, bool count_next = false);
 cudaError_t launch_sort_prep(const BpScratch& s, const uint32_t* keys, const uint32_t* count_ptr,
                              uint32_t n, int passes, cudaStream_t st);
 cudaError_t launch_sweep(const BpScratch& s, const BpArgs& a, const uint32_t* keys, const uint32_t* vals,
@@ -146,13 +149,16 @@ int sm_count();
 
 // ------------------------------------------------------------ device helpers
 #ifdef __CUDACC__
-__device__ __forceinline__ uint64_t ld_acquire_u64(const uint64_t* p) {
+// Look-back words hold flag and value in one 64-bit word, so a relaxed
+// (single-copy atomic) load/store at gpu scope is enough: a reader sees the
+// old word or the whole new one, and nothing else is published through it.
+__device__ __forceinline__ uint64_t ld_lb_u64(const uint64_t* p) {
     uint64_t v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ void st_release_u64(uint64_t* p, uint64_t v) {
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+__device__ __forceinline__ void st_lb_u64(uint64_t* p, uint64_t v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
@@ -167,25 +173,40 @@ __device__ __forceinline__ uint64_t lb_word(uint32_t tag, uint64_t flag, uint32_
 // of a status table with `cols` columns.  Returns the exclusive prefix; on
 // timeout sets kErrTimeout and returns what it has (the caller still
 // publishes, so no later tile can wait forever).
+// The words of up to kLbWindow predecessors are loaded at once (independent
+// loads), then consumed in order: aggregates are summed until a prefix is
+// met; a word not yet published stops the window and is re-read.
+constexpr int kLbWindow = 8;
 __device__ __forceinline__ uint32_t lookback(uint64_t* status, uint32_t tile, uint32_t col, uint32_t cols,
                                              uint32_t tag, uint32_t spin_limit, uint32_t* err) {
     uint32_t excl = 0;
     int64_t j = (int64_t)tile - 1;
+    uint32_t spins = 0;
     while (j >= 0) {
-        uint64_t v;
-        uint32_t spins = 0;
-        while (true) {
-            v = ld_acquire_u64(status + (uint64_t)j * cols + col);
-            if ((uint32_t)(v >> 32) == tag && (v & (kFlagAgg | kFlagPrefix))) break;
+        uint64_t w[kLbWindow];
+#pragma unroll
+        for (int k = 0; k < kLbWindow; ++k)
+            w[k] = (j - k >= 0) ? ld_lb_u64(status + (uint64_t)(j - k) * cols + col) : 0ull;
+        int consumed = 0;
+        bool done = false;
+#pragma unroll
+        for (int k = 0; k < kLbWindow; ++k) {
+            if (j - k < 0) { done = true; break; }
+            const uint64_t v = w[k];
+            if (!((uint32_t)(v >> 32) == tag && (v & (kFlagAgg | kFlagPrefix)))) break;
+            excl += (uint32_t)(v & kValMask);
+            ++consumed;
+            if (v & kFlagPrefix) { done = true; break; }
+        }
+        if (done) break;
+        j -= consumed;
+        if (consumed == 0) {
             if (++spins > spin_limit) {
                 atomicOr(err, kErrTimeout);
                 return excl;
             }
             if (spins > 64) __nanosleep(64);
         }
-        excl += (uint32_t)(v & kValMask);
-        if (v & kFlagPrefix) break;
-        --j;
     }
     return excl;
 }

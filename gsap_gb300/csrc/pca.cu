@@ -53,20 +53,10 @@ __global__ void __launch_bounds__(1024) k_plan(BpScratch S, BpArgs A) {
     if (threadIdx.x == 0) S.work_start[A.num_scenes] = s_carry;
 }
 
-// ---------------------------------------------------------------- K1
-
-__global__ void __launch_bounds__(kThreads) k_pca(BpScratch S, BpArgs A, uint64_t entry_cap) {
-    __shared__ float s_red[kThreads / 32][2 * kPcaQ + 3];
-    __shared__ double s_dred[kThreads / 32][kPcaQ + 3];
-    __shared__ uint32_t s_flag;
-    __shared__ double s_pilot[3];
-    const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    uint32_t scene, b, e, wfirst, nw;
-    if (!map_work(blockIdx.x, S, A, scene, b, e, wfirst, nw)) return;
-    const uint32_t sb = scene_begin(A, scene), se = scene_end(A, scene);
-
-    // pilot = centre of the scene's first object (shift against cancellation)
-    float px = 0.f, py = 0.f, pz = 0.f;
+// Centre of the scene's first object: every work item of a scene shifts its
+// sums by it, which keeps the FP32 covariance sums free of cancellation.
+__device__ __forceinline__ void pilot_of(const BpArgs& A, uint32_t sb, uint32_t se, float& px, float& py, float& pz) {
+    px = py = pz = 0.f;
     if (se > sb) {
         float4 a = A.mn[sb];
         if (A.mode == 0) {
@@ -75,33 +65,64 @@ __global__ void __launch_bounds__(kThreads) k_pca(BpScratch S, BpArgs A, uint64_
         } else {
             px = a.x; py = a.y; pz = a.z;
         }
-        if (!isfinite(px) || !isfinite(py) || !isfinite(pz)) { px = py = pz = 0.f; }
+        if (!isfinite(px) || !isfinite(py) || !isfinite(pz)) px = py = pz = 0.f;
     }
+}
+
+// ---------------------------------------------------------------- K1
+
+__global__ void __launch_bounds__(kThreads) k_pca(BpScratch S, BpArgs A) {
+    __shared__ float s_red[kThreads / 32][2 * kPcaQ + 3];
+    const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    uint32_t scene, b, e, wfirst, nw;
+    if (!map_work(blockIdx.x, S, A, scene, b, e, wfirst, nw)) return;
+    const uint32_t sb = scene_begin(A, scene), se = scene_end(A, scene);
+
+    // pilot = centre of the scene's first object (shift against cancellation)
+    float px = 0.f, py = 0.f, pz = 0.f;
+    pilot_of(A, sb, se, px, py, pz);
+    // Covariance sums (d, d d^T) are compensated (two-sum); the extent sums
+    // (h, h h^T) only size the grid and are plain FP32 (lo stays 0).
     float hi[kPcaQ], lo[kPcaQ], hm[3] = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int q = 0; q < kPcaQ; ++q) { hi[q] = 0.f; lo[q] = 0.f; }
     bool bad = false;
-    for (uint32_t i = b + tid; i < e; i += kThreads) {
-        float4 a = A.mn[i];
-        float cx, cy, cz, hx, hy, hz;
-        if (A.mode == 0) {
-            float4 c = A.mx[i];
-            cx = 0.5f * (a.x + c.x); cy = 0.5f * (a.y + c.y); cz = 0.5f * (a.z + c.z);
-            hx = 0.5f * fabsf(c.x - a.x); hy = 0.5f * fabsf(c.y - a.y); hz = 0.5f * fabsf(c.z - a.z);
-        } else {
-            cx = a.x; cy = a.y; cz = a.z;
-            hx = hy = hz = fabsf(a.w);
-        }
-        if (!(isfinite(cx) && isfinite(cy) && isfinite(cz) && isfinite(hx) && isfinite(hy) && isfinite(hz))) {
-            bad = true;
-            continue;
-        }
-        float dx = cx - px, dy = cy - py, dz = cz - pz;
-        float v[kPcaQ] = {dx, dy, dz, dx * dx, dx * dy, dx * dz, dy * dy, dy * dz, dz * dz,
-                          hx, hy, hz, hx * hx, hx * hy, hx * hz, hy * hy, hy * hz, hz * hz};
+    constexpr int U = 4;  // objects in flight per thread
+    for (uint32_t i0 = b + tid; i0 < e; i0 += U * kThreads) {
+        float4 A4[U], B4[U];
 #pragma unroll
-        for (int q = 0; q < kPcaQ; ++q) kahan_add(hi[q], lo[q], v[q]);
-        hm[0] = fmaxf(hm[0], hx); hm[1] = fmaxf(hm[1], hy); hm[2] = fmaxf(hm[2], hz);
+        for (int u = 0; u < U; ++u) {
+            uint32_t i = i0 + u * kThreads;
+            if (i < e) {
+                A4[u] = A.mn[i];
+                B4[u] = A.mode == 0 ? A.mx[i] : A4[u];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (i0 + u * kThreads >= e) break;
+            float4 a = A4[u], c = B4[u];
+            float cx, cy, cz, hx, hy, hz;
+            if (A.mode == 0) {
+                cx = 0.5f * (a.x + c.x); cy = 0.5f * (a.y + c.y); cz = 0.5f * (a.z + c.z);
+                hx = 0.5f * fabsf(c.x - a.x); hy = 0.5f * fabsf(c.y - a.y); hz = 0.5f * fabsf(c.z - a.z);
+            } else {
+                cx = a.x; cy = a.y; cz = a.z;
+                hx = hy = hz = fabsf(a.w);
+            }
+            if (!(isfinite(cx) && isfinite(cy) && isfinite(cz) && isfinite(hx) && isfinite(hy) && isfinite(hz))) {
+                bad = true;
+                continue;
+            }
+            float dx = cx - px, dy = cy - py, dz = cz - pz;
+            const float v[9] = {dx, dy, dz, dx * dx, dx * dy, dx * dz, dy * dy, dy * dz, dz * dz};
+#pragma unroll
+            for (int q = 0; q < 9; ++q) kahan_add(hi[q], lo[q], v[q]);
+            const float w[9] = {hx, hy, hz, hx * hx, hx * hy, hx * hz, hy * hy, hy * hz, hz * hz};
+#pragma unroll
+            for (int q = 0; q < 9; ++q) hi[9 + q] += w[q];
+            hm[0] = fmaxf(hm[0], hx); hm[1] = fmaxf(hm[1], hy); hm[2] = fmaxf(hm[2], hz);
+        }
     }
     if (bad) atomicOr(&S.ctrl->error, kErrNonFinite);
     // warp, then CTA, compensated reduction
@@ -132,61 +153,82 @@ __global__ void __launch_bounds__(kThreads) k_pca(BpScratch S, BpArgs A, uint64_
         for (int w = 1; w < kThreads / 32; ++w) m = fmaxf(m, s_red[w][2 * kPcaQ + k]);
         S.partials[blockIdx.x].hmax[k] = m;
     }
-    // last work item of the scene combines
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) {
-        uint32_t old = atomicAdd(&S.scene_done[scene], 1u);
-        s_flag = (old == nw - 1) ? 1u : 0u;
-        s_pilot[0] = px; s_pilot[1] = py; s_pilot[2] = pz;
-    }
-    __syncthreads();
-    if (!s_flag) return;
-    __threadfence();
-    // FP64 combine of the scene's partials: thread t takes items t, t+256, ...
-    double acc[kPcaQ + 3];
+}
+
+// K1b: one CTA per scene combines the scene's partials in FP64 (fixed order:
+// deterministic), solves the 3x3 eigenproblem and picks the grid; the last
+// scene to finish computes the global bucket bases and the key layout and
+// resets the counters of the later stages.  A separate launch keeps the FP64
+// tail's registers out of the streaming kernel.
+__global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, uint64_t entry_cap) {
+    __shared__ uint32_t s_flag;
+    const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const uint32_t scene = blockIdx.x;
+    if (scene >= A.num_scenes) return;
+    const uint32_t sb = scene_begin(A, scene), se = scene_end(A, scene);
+    const uint32_t wfirst = A.scene_off ? S.work_start[scene] : 0u;
+    const uint32_t nw = A.scene_off ? S.work_start[scene + 1] - wfirst : work_items(A.n);
+    // Combine the scene's partials in float-float (two-sum) arithmetic on the
+    // FP32 pipes: thread t merges items t, t+256, ..., then warps and the CTA
+    // merge in a fixed order (deterministic); only the final hi + lo pairs go
+    // to FP64 (GB300's FP64 lane rate makes an FP64 reduction tree slow).
+    float ah[kPcaQ], al[kPcaQ], am[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-    for (int q = 0; q < kPcaQ + 3; ++q) acc[q] = 0.0;
+    for (int q = 0; q < kPcaQ; ++q) { ah[q] = 0.f; al[q] = 0.f; }
     for (uint32_t k = tid; k < nw; k += kThreads) {
         const PcaPartial* P = &S.partials[wfirst + k];
 #pragma unroll
-        for (int q = 0; q < kPcaQ; ++q) acc[q] += (double)__ldcg(&P->hi[q]) + (double)__ldcg(&P->lo[q]);
+        for (int q = 0; q < kPcaQ; ++q) kahan_merge(ah[q], al[q], P->hi[q], P->lo[q]);
 #pragma unroll
-        for (int q = 0; q < 3; ++q) acc[kPcaQ + q] = fmax(acc[kPcaQ + q], (double)__ldcg(&P->hmax[q]));
+        for (int q = 0; q < 3; ++q) am[q] = fmaxf(am[q], P->hmax[q]);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
-        for (int q = 0; q < kPcaQ; ++q) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], o);
+        for (int q = 0; q < kPcaQ; ++q) {
+            float h2 = __shfl_down_sync(0xffffffffu, ah[q], o);
+            float l2 = __shfl_down_sync(0xffffffffu, al[q], o);
+            kahan_merge(ah[q], al[q], h2, l2);
+        }
 #pragma unroll
-        for (int q = kPcaQ; q < kPcaQ + 3; ++q) acc[q] = fmax(acc[q], __shfl_down_sync(0xffffffffu, acc[q], o));
+        for (int q = 0; q < 3; ++q) am[q] = fmaxf(am[q], __shfl_down_sync(0xffffffffu, am[q], o));
     }
-    if (lane == 0)
-        for (int q = 0; q < kPcaQ + 3; ++q) s_dred[wid][q] = acc[q];
+    __shared__ float s_ff[kThreads / 32][2 * kPcaQ + 3];
+    __shared__ double s_tot[kPcaQ + 3];
+    if (lane == 0) {
+        for (int q = 0; q < kPcaQ; ++q) { s_ff[wid][q] = ah[q]; s_ff[wid][kPcaQ + q] = al[q]; }
+        for (int q = 0; q < 3; ++q) s_ff[wid][2 * kPcaQ + q] = am[q];
+    }
     __syncthreads();
+    if (tid < kPcaQ) {
+        float h = s_ff[0][tid], l = s_ff[0][kPcaQ + tid];
+        for (int w = 1; w < kThreads / 32; ++w) kahan_merge(h, l, s_ff[w][tid], s_ff[w][kPcaQ + tid]);
+        s_tot[tid] = (double)h + (double)l;
+    } else if (tid < kPcaQ + 3) {
+        float m = s_ff[0][2 * kPcaQ + tid - kPcaQ];
+        for (int w = 1; w < kThreads / 32; ++w) m = fmaxf(m, s_ff[w][2 * kPcaQ + tid - kPcaQ]);
+        s_tot[tid] = (double)m;
+    }
+    __syncthreads();
+    Ctrl* C = S.ctrl;
     if (tid == 0) {
         SceneSums z;
-        double t[kPcaQ + 3];
-        for (int q = 0; q < kPcaQ + 3; ++q) {
-            double v = s_dred[0][q];
-            for (int w = 1; w < kThreads / 32; ++w)
-                v = (q < kPcaQ) ? v + s_dred[w][q] : fmax(v, s_dred[w][q]);
-            t[q] = v;
-        }
+        const double* t = s_tot;
         for (int k = 0; k < 3; ++k) { z.sd[k] = t[k]; z.sh[k] = t[9 + k]; z.hmax[k] = t[kPcaQ + k]; }
         for (int k = 0; k < 6; ++k) { z.sdd[k] = t[3 + k]; z.shh[k] = t[12 + k]; }
-        for (int k = 0; k < 3; ++k) z.pilot[k] = s_pilot[k];
+        float px = 0.f, py = 0.f, pz = 0.f;
+        pilot_of(A, sb, se, px, py, pz);
+        z.pilot[0] = px; z.pilot[1] = py; z.pilot[2] = pz;
         z.n = (double)(se - sb);
         Scene sc;
         choose_scene(z, A, entry_cap, A.n, sc);
         S.scenes[scene] = sc;
-        S.scene_done[scene] = 0u;  // self-reset for the next call
         __threadfence();
-        uint32_t old = atomicAdd(&S.ctrl->scenes_done, 1u);
-        s_flag = (old == A.num_scenes - 1) ? 2u : 0u;
+        uint32_t old = atomicAdd(&C->scenes_done, 1u);
+        s_flag = (old == A.num_scenes - 1) ? 1u : 0u;
     }
     __syncthreads();
-    if (s_flag != 2u) return;
+    if (!s_flag) return;
     __threadfence();
     // Last scene: global bucket bases, key layout, and counter reset.
     __shared__ uint32_t s_wsum[kThreads / 32];
@@ -212,7 +254,7 @@ __global__ void __launch_bounds__(kThreads) k_pca(BpScratch S, BpArgs A, uint64_
         if (tid == kThreads - 1) s_carry = excl + v;
         __syncthreads();
     }
-    Ctrl* C = S.ctrl;
+    __shared__ uint32_t s_q;
     if (tid == 0) {
         uint32_t total = s_carry;
         uint32_t bbits = 0;
@@ -220,6 +262,7 @@ __global__ void __launch_bounds__(kThreads) k_pca(BpScratch S, BpArgs A, uint64_
         uint32_t q = A.key_bits > bbits ? A.key_bits - bbits : 0u;
         if (q > 24) q = 24;
         if (q == 0) atomicOr(&C->error, kErrCellRange);
+        s_q = q;
         C->qbits = q;
         C->key_bits = A.key_bits;
         C->total_buckets = total;
@@ -231,10 +274,15 @@ __global__ void __launch_bounds__(kThreads) k_pca(BpScratch S, BpArgs A, uint64_
         C->scan_total = 0;
         C->long_rows = 0;
         C->tests = 0ull;
+        C->iters = 0ull;
         C->epoch = C->epoch + 1u;
         C->scenes_done = 0;
     }
     for (int p = 0; p < kMaxPasses; ++p) C->hist[p][tid] = 0u;
+    __syncthreads();
+    // quantisation scale of every scene, computed once for all kernels
+    const float qf = (float)(1u << s_q);
+    for (uint32_t s = tid; s < A.num_scenes; s += kThreads) S.scenes[s].q_scale = __fdiv_rn(qf, __ldcg(&S.scenes[s].q_range));
 }
 
 cudaError_t launch_plan(const BpScratch& s, const BpArgs& a, cudaStream_t st) {
@@ -243,7 +291,8 @@ cudaError_t launch_plan(const BpScratch& s, const BpArgs& a, cudaStream_t st) {
 }
 
 cudaError_t launch_pca(const BpScratch& s, const BpArgs& a, cudaStream_t st) {
-    k_pca<<<a.num_work, kThreads, 0, st>>>(s, a, s.entry_cap);
+    k_pca<<<a.num_work, kThreads, 0, st>>>(s, a);
+    k_pca_finish<<<a.num_scenes, kThreads, 0, st>>>(s, a, s.entry_cap);
     return cudaGetLastError();
 }
 

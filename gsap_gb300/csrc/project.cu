@@ -1,5 +1,6 @@
 // K2: projection of every object onto the scene's axes, cell replication
-// and the radix histograms of the first sort.
+// and the histogram of the first radix digit (each sort pass counts the next
+// digit while it has its tile staged in shared memory).
 //
 // Replaces projectSubMultiple (sapDetection/SapKernel.cu:151-213, key =
 // u.c - r + quadrant * interval, id = i) and the 8x4 cell mask of
@@ -51,7 +52,8 @@ __device__ __forceinline__ bool load_box(const BpArgs& A, uint32_t i, float3& a,
     return isfinite(a.x) && isfinite(a.y) && isfinite(a.z) && isfinite(b.x) && isfinite(b.y) && isfinite(b.z);
 }
 
-constexpr int kProjItems = kChunk / kThreads;  // 16 objects per thread
+constexpr int kProjItems = 8;                          // objects per thread per half
+constexpr int kProjHalf = kThreads * kProjItems;       // a chunk is processed in two halves
 
 template <int PASSES>
 __global__ void __launch_bounds__(kThreads) k_project(BpScratch S, BpArgs A) {
@@ -69,7 +71,7 @@ __global__ void __launch_bounds__(kThreads) k_project(BpScratch S, BpArgs A) {
         for (int k = 0; k < 9; ++k) s_f[k] = sc.u[k];
         uint32_t Q = S.ctrl->qbits;
         s_f[9] = sc.q_org;
-        s_f[10] = __fdiv_rn((float)(1u << Q), sc.q_range);
+        s_f[10] = sc.q_scale;
         s_f[11] = sc.c2_org;
         s_f[12] = sc.c2_inv;
         s_f[13] = sc.c3_org;
@@ -83,10 +85,11 @@ __global__ void __launch_bounds__(kThreads) k_project(BpScratch S, BpArgs A) {
     const uint32_t G2 = s_i[0], G3 = s_i[1], bb = s_i[2], Q = s_i[3];
     const float qmax = (float)((1u << Q) - 1u);
 
+    bool bad = false;
+    for (int half = 0; half < kChunk / kProjHalf; ++half) {
     uint32_t qlo[kProjItems], clo[kProjItems], ncl[kProjItems], pre[kProjItems];
     uint32_t running = 0;
-    bool bad = false;
-    const uint32_t wb = b + wid * (32 * kProjItems);
+    const uint32_t wb = b + half * kProjHalf + wid * (32 * kProjItems);
 #pragma unroll
     for (int k = 0; k < kProjItems; ++k) {
         uint32_t i = wb + k * 32 + lane;
@@ -122,7 +125,6 @@ __global__ void __launch_bounds__(kThreads) k_project(BpScratch S, BpArgs A) {
         pre[k] = running + x - r;
         running += __shfl_sync(0xffffffffu, x, 31);
     }
-    if (bad) atomicOr(&S.ctrl->error, kErrNonFinite);
     if (lane == 0) s_wtot[wid] = running;
     __syncthreads();
     if (tid == 0) {
@@ -147,15 +149,17 @@ __global__ void __launch_bounds__(kThreads) k_project(BpScratch S, BpArgs A) {
                 if (pos < S.entry_cap) {  // entries past the capacity are counted, never stored
                     S.keys[0][pos] = key;
                     S.vals[0][pos] = i;
-#pragma unroll
-                    for (int p = 0; p < PASSES; ++p) atomicAdd(&s_hist[p][(key >> (8 * p)) & 255u], 1u);
+                    atomicAdd(&s_hist[0][key & 255u], 1u);  // later digits: counted by the sort passes
                 }
             }
     }
+    __syncthreads();  // s_wtot / s_base are reused by the next half
+    }
+    if (bad) atomicOr(&S.ctrl->error, kErrNonFinite);
     __syncthreads();
-    for (uint32_t k = tid; k < PASSES * 256; k += kThreads) {
-        uint32_t v = (&s_hist[0][0])[k];
-        if (v) atomicAdd(&S.ctrl->hist[0][0] + k, v);
+    for (uint32_t k = tid; k < 256; k += kThreads) {
+        uint32_t v = s_hist[0][k];
+        if (v) atomicAdd(&S.ctrl->hist[0][k], v);
     }
 }
 

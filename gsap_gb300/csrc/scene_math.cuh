@@ -6,8 +6,9 @@
 // symmetric eigensolve.  The solve runs a cyclic Jacobi in FP32 first (FP32
 // rotations are cheap on the GPU, FP64 ones are not) and then polishes in
 // FP64: B = V32^T C V32 is formed in FP64 and diagonalised by FP64 Jacobi
-// rotations until its off-diagonal part is below 1e-17 of its diagonal, which
-// takes one or two sweeps because B is already nearly diagonal.  The
+// rotations until its off-diagonal part reaches rounding level (~2 ulps of
+// the diagonal), which takes one or two sweeps because B is already nearly
+// diagonal.  The
 // eigenvectors are V32 W in FP64.  The grid choice that follows is a
 // heuristic (any grid gives the same pair set) and runs in FP32.
 #pragma once
@@ -49,12 +50,18 @@ __host__ __device__ inline void jacobi_rotate(T a[3][3], T v[3][3], int p, int q
     }
 }
 
+// Sweeps until the off-diagonal part is below tol * |diag| or stops
+// shrinking (it cannot go below a few ulps of the diagonal, so a tolerance
+// under the type's epsilon would otherwise run every sweep).
 template <class T>
 __host__ __device__ inline void jacobi_sweeps(T a[3][3], T v[3][3], T tol, int max_sweeps) {
     const T scale = fabs(a[0][0]) + fabs(a[1][1]) + fabs(a[2][2]) + T(1e-30);
+    T prev = T(-1);
     for (int sweep = 0; sweep < max_sweeps; ++sweep) {
         T off = fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]);
         if (off <= tol * scale) break;
+        if (prev >= T(0) && off >= T(0.5) * prev) break;  // converged to rounding level
+        prev = off;
         jacobi_rotate(a, v, 0, 1);
         jacobi_rotate(a, v, 0, 2);
         jacobi_rotate(a, v, 1, 2);
@@ -70,7 +77,7 @@ __host__ __device__ inline void eig3(double a[3][3], double v[3][3]) {
             af[i][j] = (float)a[i][j];
             vf[i][j] = (i == j) ? 1.f : 0.f;
         }
-    jacobi_sweeps<float>(af, vf, 1e-7f, 12);
+    jacobi_sweeps<float>(af, vf, 2.4e-7f, 12);
     // B = V32^T A V32 in FP64
     double V[3][3], t[3][3], b[3][3];
     // re-orthonormalise the FP32 basis in FP64 (Gram-Schmidt, third column
@@ -99,7 +106,7 @@ __host__ __device__ inline void eig3(double a[3][3], double v[3][3]) {
     double w[3][3];
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) w[i][j] = (i == j) ? 1.0 : 0.0;
-    jacobi_sweeps<double>(b, w, 1e-17, 16);
+    jacobi_sweeps<double>(b, w, 4.4e-16, 16);
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) {
             v[i][j] = V[i][0] * w[0][j] + V[i][1] * w[1][j] + V[i][2] * w[2][j];

@@ -4,12 +4,13 @@
 // (sapDetection/radixsort.cu:1116-1348 radixSortStep: per pass a 1024-key
 // CTA-local split sort, findRadixOffsets, a CUDPP scan of the counters and
 // reorderData, i.e. four launches and a library scan per 4-bit digit).
-// Here every pass is one launch: the digit histograms of all passes were
-// counted up front (fused into the projection kernel), each CTA ranks a
-// 4096-key tile with warp ballots (eight ballots give every lane the mask of
-// lanes holding the same digit), publishes its per-digit counts, and finds
-// its global offsets by a decoupled look-back over earlier tiles.  Tiles are
-// handed out in order by an atomic counter, so a tile only ever waits on
+// Here every pass is one launch: the first digit's histogram is counted by
+// the projection kernel and each pass counts the next digit's while its tile
+// sits in shared memory; each CTA ranks a 4096-key tile with warp ballots
+// (eight ballots give every lane the mask of lanes holding the same digit),
+// publishes its per-digit counts, and finds its global offsets by a
+// decoupled look-back over earlier tiles (one thread per digit, eight
+// predecessor words per round trip).  Tiles are handed out in order by an atomic counter, so a tile only ever waits on
 // tiles that running CTAs own; every wait is bounded and reports
 // GSAP_ERR_DEVICE_TIMEOUT instead of hanging.  Stable: equal digits keep
 // their input order, so the passes give the order of a stable sort.
@@ -37,13 +38,14 @@ __device__ __forceinline__ uint32_t cta_excl_scan256(uint32_t v, uint32_t* s_w) 
 }
 
 template <int ITEMS>
-__global__ void __launch_bounds__(kThreads) k_onesweep(BpScratch S, const uint32_t* __restrict__ kin,
+__global__ void __launch_bounds__(kThreads, 2) k_onesweep(BpScratch S, const uint32_t* __restrict__ kin,
                                                        const uint32_t* __restrict__ vin,
                                                        uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
                                                        const uint32_t* count_ptr, uint32_t cap, int pass,
-                                                       uint32_t spin, SortGather G) {
+                                                       uint32_t spin, SortGather G, int count_next) {
     constexpr int TILE = kThreads * ITEMS;
     __shared__ uint32_t s_k[TILE];
+    __shared__ uint32_t s_next[256];  // histogram of the next pass's digit over this tile
     __shared__ uint32_t s_v[TILE];
     __shared__ uint32_t s_wh[kThreads / 32][256];
     __shared__ uint32_t s_gdig[256];
@@ -64,76 +66,93 @@ __global__ void __launch_bounds__(kThreads) k_onesweep(BpScratch S, const uint32
         if (tid == 0) s_tile = atomicAdd(&S.ctrl->tile_ctr[pass], 1u);
 #pragma unroll
         for (int w = 0; w < kThreads / 32; ++w) s_wh[w][tid] = 0u;
+        s_next[tid] = 0u;
         __syncthreads();
         const uint32_t t = s_tile;
         if (t >= ntiles) break;
         const uint32_t tbase = t * TILE;
         const uint32_t wb = tbase + wid * 32 * ITEMS;
-        uint32_t key[ITEMS], val[ITEMS], rk[ITEMS];
-#pragma unroll
-        for (int k = 0; k < ITEMS; ++k) {
-            uint32_t idx = wb + k * 32 + lane;
-            if (idx < n) {
-                key[k] = __ldcs(kin + idx);
-                val[k] = __ldcs(vin + idx);
-            } else {
-                key[k] = 0u;
-                val[k] = 0u;
-            }
-        }
-        // warp-level multi-split ranking, items in index order
-#pragma unroll
-        for (int k = 0; k < ITEMS; ++k) {
-            const bool valid = wb + k * 32 + lane < n;
-            const uint32_t d = (key[k] >> shift) & 255u;
-            uint32_t m = __ballot_sync(0xffffffffu, valid);
-#pragma unroll
-            for (int bit = 0; bit < 8; ++bit) {
-                uint32_t bal = __ballot_sync(0xffffffffu, (d >> bit) & 1u);
-                m &= ((d >> bit) & 1u) ? bal : ~bal;
-            }
-            uint32_t before = valid ? s_wh[wid][d] : 0u;
-            uint32_t r = __popc(m & lt);
-            __syncwarp();
-            if (valid && r == 0) s_wh[wid][d] = before + __popc(m);
-            __syncwarp();
-            rk[k] = before + r;
-        }
-        __syncthreads();
-        // per digit: exclusive warp offsets and the tile count
         uint32_t tot = 0;
+        {
+            uint32_t key[ITEMS], val[ITEMS], rk[ITEMS];
 #pragma unroll
-        for (int w = 0; w < kThreads / 32; ++w) {
-            uint32_t c = s_wh[w][tid];
-            s_wh[w][tid] = tot;
-            tot += c;
+            for (int k = 0; k < ITEMS; ++k) {
+                uint32_t idx = wb + k * 32 + lane;
+                if (idx < n) {
+                    key[k] = __ldcs(kin + idx);
+                    val[k] = __ldcs(vin + idx);
+                } else {
+                    key[k] = 0u;
+                    val[k] = 0u;
+                }
+            }
+            // warp-level multi-split ranking, items in index order
+#pragma unroll
+            for (int k = 0; k < ITEMS; ++k) {
+                const bool valid = wb + k * 32 + lane < n;
+                const uint32_t d = (key[k] >> shift) & 255u;
+                uint32_t m = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+                for (int bit = 0; bit < 8; ++bit) {
+                    uint32_t bal = __ballot_sync(0xffffffffu, (d >> bit) & 1u);
+                    m &= ((d >> bit) & 1u) ? bal : ~bal;
+                }
+                uint32_t before = valid ? s_wh[wid][d] : 0u;
+                uint32_t r = __popc(m & lt);
+                __syncwarp();
+                if (valid && r == 0) s_wh[wid][d] = before + __popc(m);
+                __syncwarp();
+                rk[k] = before + r;
+            }
+            __syncthreads();
+            // per digit: exclusive warp offsets and the tile count
+#pragma unroll
+            for (int w = 0; w < kThreads / 32; ++w) {
+                uint32_t c = s_wh[w][tid];
+                s_wh[w][tid] = tot;
+                tot += c;
+            }
+            // publish the aggregates before anything else
+            st_lb_u64(S.status + (uint64_t)t * 256u + tid, lb_word(tag, t == 0 ? kFlagPrefix : kFlagAgg, tot));
+            s_start[tid] = cta_excl_scan256(tot, s_scan);
+            __syncthreads();  // every digit's tile start is read below by other threads
+            // stage the tile in digit order (frees the registers for the look-back)
+#pragma unroll
+            for (int k = 0; k < ITEMS; ++k) {
+                if (wb + k * 32 + lane < n) {
+                    uint32_t d = (key[k] >> shift) & 255u;
+                    uint32_t lp = s_start[d] + s_wh[wid][d] + rk[k];
+                    if (lp < (uint32_t)TILE) {
+                        s_k[lp] = key[k];
+                        s_v[lp] = val[k];
+                    } else {
+                        atomicOr(&S.ctrl->error, kErrInternal);
+                    }
+                }
+            }
         }
-        uint64_t* st = S.status + (uint64_t)t * 256u + tid;
-        st_release_u64(st, lb_word(tag, t == 0 ? kFlagPrefix : kFlagAgg, tot));
-        s_start[tid] = cta_excl_scan256(tot, s_scan);
         uint32_t excl = 0;
         if (t > 0) {
             excl = lookback(S.status, t, tid, 256u, tag, spin, &S.ctrl->error);
-            st_release_u64(st, lb_word(tag, kFlagPrefix, excl + tot));
+            st_lb_u64(S.status + (uint64_t)t * 256u + tid, lb_word(tag, kFlagPrefix, excl + tot));
         }
         s_gb[tid] = s_gdig[tid] + excl - s_start[tid];
         __syncthreads();
-        // stage the tile in digit order
-#pragma unroll
-        for (int k = 0; k < ITEMS; ++k) {
-            if (wb + k * 32 + lane < n) {
-                uint32_t d = (key[k] >> shift) & 255u;
-                uint32_t lp = s_start[d] + s_wh[wid][d] + rk[k];
-                s_k[lp] = key[k];
-                s_v[lp] = val[k];
-            }
-        }
-        __syncthreads();
         const uint32_t tn = min((uint32_t)TILE, n - tbase);
+        if (count_next) {  // the next pass's digit histogram, counted here instead of up front
+            for (uint32_t i = tid; i < tn; i += kThreads) atomicAdd(&s_next[(s_k[i] >> (shift + 8)) & 255u], 1u);
+            __syncthreads();
+            const uint32_t c = s_next[tid];
+            if (c) atomicAdd(&S.ctrl->hist[pass + 1][tid], c);
+        }
         for (uint32_t i = tid; i < tn; i += kThreads) {
             uint32_t kk = s_k[i];
             uint32_t g = s_gb[(kk >> shift) & 255u] + i;
             uint32_t vv = s_v[i];
+            if (g >= n) {  // cannot happen with consistent counts; never write out of range
+                atomicOr(&S.ctrl->error, kErrInternal);
+                continue;
+            }
             kout[g] = kk;
             vout[g] = vv;
             if (G.smin) {  // last pass of the broadphase: entries in sorted order
@@ -190,8 +209,7 @@ cudaError_t launch_sort_prep(const BpScratch& s, const uint32_t* keys, const uin
 
 cudaError_t launch_sort_pass(const BpScratch& s, int pass, int passes, const uint32_t* kin, const uint32_t* vin,
                              uint32_t* kout, uint32_t* vout, const uint32_t* count_ptr, uint64_t cap,
-                             uint32_t spin, cudaStream_t st, const SortGather* gather) {
-    (void)passes;
+                             uint32_t spin, cudaStream_t st, const SortGather* gather, bool count_next) {
     SortGather G;
     if (gather) G = *gather;
     else G = SortGather{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -202,7 +220,8 @@ cudaError_t launch_sort_pass(const BpScratch& s, int pass, int passes, const uin
         grid = sm_count() * (per_sm > 0 ? per_sm : 1);
     }
     uint32_t c = cap > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)cap;
-    k_onesweep<kSortItems><<<grid, kThreads, 0, st>>>(s, kin, vin, kout, vout, count_ptr, c, pass, spin, G);
+    const int next = (count_next && pass + 1 < passes) ? 1 : 0;
+    k_onesweep<kSortItems><<<grid, kThreads, 0, st>>>(s, kin, vin, kout, vout, count_ptr, c, pass, spin, G, next);
     return cudaGetLastError();
 }
 

@@ -9,7 +9,8 @@
 // and the cross pass of SapKernel.cu:2364-2446.
 //
 // Persistent warps take 32 consecutive sorted entries at a time from an
-// atomic counter (work stealing).  Each lane scans forward from its entry
+// atomic counter (work stealing).  Each lane scans forward from its entry,
+// kUnroll candidates per iteration with their loads issued together,
 // while the candidate key is <= (bucket | q(hi1)): the q map is monotone, so
 // every later entry of the same cell whose interval on u1 can meet this one
 // is visited, and the scan stops at the cell (and scene) boundary by
@@ -36,7 +37,8 @@ __device__ __forceinline__ float proj_hi(const float* u, float3 a, float3 b) {
     return __fadd_ru(__fadd_ru(h0, h1), h2);
 }
 
-constexpr int kBuf = 128;
+constexpr int kBuf = 128;  // pairs buffered per warp before a global reservation
+constexpr int kUnroll = 4; // candidates per lane per iteration (loads issued together)
 
 template <int MODE>
 __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const uint32_t* __restrict__ keys,
@@ -54,7 +56,7 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
     const uint32_t qmask = (1u << Q) - 1u;
     const float qmax = (float)qmask;
     uint32_t nbuf = 0;
-    unsigned long long tests = 0;
+    uint32_t my_tests = 0, iters = 0;
 
     auto flush = [&]() {
         __syncwarp();
@@ -82,13 +84,12 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
         if (base >= E) break;
         const uint32_t e = base + lane;
         bool live = e < E;
-        uint32_t i = 0, kb = 0, c2 = 0, c3 = 0, ci = 0;
+        uint32_t i = 0, kb = 0, bucket = 0, ci = 0, bbase = 0, g3 = 1;
         float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), pb = pa;
         if (live) {
             const uint32_t key = keys[e];
             i = vals[e];
-            const uint32_t s = S.objscene ? S.objscene[i] : 0u;
-            const Scene* sc = &S.scenes[s];
+            const Scene* sc = &S.scenes[S.objscene ? S.objscene[i] : 0u];
             pa = smin[e];
             float3 a, b;
             if (MODE == 0) {
@@ -102,59 +103,82 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
             }
             float u[3] = {sc->u[0], sc->u[1], sc->u[2]};
             float h1 = proj_hi(u, a, b);
-            float qs = __fdiv_rn((float)(1u << Q), sc->q_range);
-            float t = __fmul_rn(__fsub_rn(h1, sc->q_org), qs);
+            float t = __fmul_rn(__fsub_rn(h1, sc->q_org), sc->q_scale);
             uint32_t qh = (uint32_t)fminf(fmaxf(t, 0.f), qmax);
             kb = (key & ~qmask) | qh;
-            uint32_t local = (key >> Q) - sc->bucket_base;
-            uint32_t G3 = sc->G3;
-            c2 = local / G3;
-            c3 = local - c2 * G3;
+            bucket = key >> Q;
+            bbase = sc->bucket_base;
+            g3 = sc->G3;
             ci = scell[e];
         }
         uint32_t j = e + 1;
         while (true) {
-            bool act = live && j < E;
-            if (act) act = __ldg(keys + j) <= kb;
-            live = act;
-            const uint32_t am = __ballot_sync(0xffffffffu, act);
-            if (!am) break;
-            tests += __popc(am);
-            bool hit = false;
-            uint32_t o = 0;
-            if (act) {
-                float4 qa = __ldg(smin + j);
-                bool ov;
-                if (MODE == 0) {
-                    float4 qb = __ldg(smax + j);
-                    ov = pa.x <= qb.x && qa.x <= pb.x && pa.y <= qb.y && qa.y <= pb.y && pa.z <= qb.z &&
-                         qa.z <= pb.z;
-                } else {
-                    float dx = __fsub_rn(pa.x, qa.x), dy = __fsub_rn(pa.y, qa.y), dz = __fsub_rn(pa.z, qa.z);
-                    float t1 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-                    float r = __fadd_rn(pa.w, qa.w);
-                    ov = t1 < __fmul_rn(r, r);
+            // the next kUnroll candidates: keys are sorted, so the active ones form a prefix
+            bool act[kUnroll];
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) {
+                const uint32_t jj = j + u;
+                act[u] = live && jj < E && __ldg(keys + jj) <= kb;
+            }
+#pragma unroll
+            for (int u = 1; u < kUnroll; ++u) act[u] = act[u] && act[u - 1];
+            if (!__any_sync(0xffffffffu, act[0])) break;
+            ++iters;
+            float4 qa[kUnroll], qb[kUnroll];
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u)
+                if (act[u]) {
+                    qa[u] = __ldg(smin + j + u);
+                    if (MODE == 0) qb[u] = __ldg(smax + j + u);
                 }
-                if (ov) {
-                    uint32_t co = __ldg(scell + j);
-                    if (max(ci >> 16, co >> 16) == c2 && max(ci & 0xFFFFu, co & 0xFFFFu) == c3) {
-                        hit = true;
-                        o = __ldg(vals + j);
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) {
+                bool hit = false;
+                uint32_t o = 0;
+                if (act[u]) {
+                    ++my_tests;
+                    bool ov;
+                    if (MODE == 0) {
+                        ov = (pa.x <= qb[u].x) & (qa[u].x <= pb.x) & (pa.y <= qb[u].y) & (qa[u].y <= pb.y) &
+                             (pa.z <= qb[u].z) & (qa[u].z <= pb.z);
+                    } else {
+                        float dx = __fsub_rn(pa.x, qa[u].x), dy = __fsub_rn(pa.y, qa[u].y),
+                              dz = __fsub_rn(pa.z, qa[u].z);
+                        float t1 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                        float r = __fadd_rn(pa.w, qa[u].w);
+                        ov = t1 < __fmul_rn(r, r);
+                    }
+                    if (ov) {
+                        // owner-cell rule: the pair belongs to the cell of (max lo2, max lo3)
+                        const uint32_t co = __ldg(scell + j + u);
+                        const uint32_t own = bbase + max(ci >> 16, co >> 16) * g3 + max(ci & 0xFFFFu, co & 0xFFFFu);
+                        if (own == bucket) {
+                            hit = true;
+                            o = __ldg(vals + j + u);
+                        }
                     }
                 }
+                const uint32_t hm = __ballot_sync(0xffffffffu, hit);
+                if (hm) {
+                    const uint32_t cnt = __popc(hm);
+                    if (nbuf + cnt > kBuf) flush();
+                    if (hit) s_buf[wid][nbuf + __popc(hm & lt)] = make_uint2(min(i, o), max(i, o));
+                    nbuf += cnt;
+                }
             }
-            uint32_t hm = __ballot_sync(0xffffffffu, hit);
-            if (hm) {
-                uint32_t cnt = __popc(hm);
-                if (nbuf + cnt > kBuf) flush();
-                if (hit) s_buf[wid][nbuf + __popc(hm & lt)] = make_uint2(min(i, o), max(i, o));
-                nbuf += cnt;
-            }
-            ++j;
+            live = act[kUnroll - 1];
+            j += kUnroll;
         }
     }
     flush();
-    if (lane == 0 && tests) atomicAdd(&C->tests, tests);
+    // diagnostics: candidate tests and warp iterations of this warp
+    uint32_t t = my_tests;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
+    if (lane == 0 && t) {
+        atomicAdd(&C->tests, (unsigned long long)t);
+        atomicAdd(&C->iters, (unsigned long long)iters);
+    }
 }
 
 cudaError_t launch_sweep(const BpScratch& s, const BpArgs& a, const uint32_t* keys, const uint32_t* vals,

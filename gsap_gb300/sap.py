@@ -179,7 +179,7 @@ class Sap:
         if load().gsap_debug_stats(self._h, out, C.c_void_p(_stream_ptr(stream))) != 0:
             raise GsapError(3, "stats read failed")
         v = list(out)
-        return dict(zip(("entries", "tests", "pairs", "buckets", "qbits", "long_rows", "key_bits", "error"), v))
+        return dict(zip(("entries", "tests", "pairs", "buckets", "qbits", "long_rows", "iters", "error"), v))
 
     def enable_timing(self, on: bool = True):
         load().gsap_sap_enable_timing(self._h, int(on))

@@ -21,7 +21,8 @@ int gsap_debug_scene_solve(const double* sums18, const double* hmax3, const doub
 
 /* Counters of the last broadphase call of a handle (synchronizes):
  * out8 = sweep entries, candidate tests, pairs, buckets, q bits, long rows
- * of the canonical sort, key bits, device error word.  Returns 0. */
+ * of the canonical sort, warp iterations of the sweep loop, device error
+ * word.  Returns 0. */
 struct gsap_sap;
 int gsap_debug_stats(struct gsap_sap* h, uint64_t* out8, void* stream);
 
