@@ -63,6 +63,7 @@ SIGNATURES = [
     ("gsap_sap_stage_times", C.c_int, [P, C.POINTER(F32), C.c_int]),
     ("gsap_sap_enable_timing", None, [P, C.c_int]),
     ("gsap_radix_sort_u32", I32, [P, P, P, U32, U32, P]),
+    ("gsap_radix_sort_u32_noalloc", I32, [P, P, U32, U32, P]),
     ("gsap_rb_create", P, [I32, I32, I32]),
     ("gsap_rb_destroy", None, [P]),
     ("gsap_rb_set_body_data", I32, [P, C.POINTER(BodyData)]),

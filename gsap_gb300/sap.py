@@ -38,6 +38,23 @@ def _dev_ptr(t: torch.Tensor | None, name: str, dtype=None, cols=None) -> int | 
     return t.data_ptr()
 
 
+NOALLOC_SORT_MAX_N = 1 << 20  # GSAP_NOALLOC_SORT_MAX_N
+
+
+def radix_sort_noalloc(keys: torch.Tensor, vals: torch.Tensor | None = None, bits: int = 32, stream=None):
+    """In-place stable sort like ``Sap.radix_sort`` that allocates no device
+    memory and needs no handle: its scratch is a fixed static device array,
+    so at most ``NOALLOC_SORT_MAX_N`` keys, and calls that overlap in time
+    race.  The first call on a device does a synchronising set-up."""
+    _dev_ptr(keys, "keys", torch.int32)
+    _dev_ptr(vals, "vals", torch.int32)
+    if vals is not None and vals.numel() != keys.numel():
+        raise ValueError("keys and vals must have the same length")
+    check(load().gsap_radix_sort_u32_noalloc(keys.data_ptr(), vals.data_ptr() if vals is not None else None,
+                                             C.c_uint32(keys.numel()), C.c_uint32(bits),
+                                             C.c_void_p(_stream_ptr(stream))))
+
+
 class Sap:
     """GB300 sweep-and-prune broadphase handle (owns all scratch)."""
 

@@ -155,6 +155,24 @@ void gsap_sap_enable_timing(gsap_sap* h, int enable);
 gsap_status gsap_radix_sort_u32(gsap_sap* h, uint32_t* d_keys, uint32_t* d_vals, uint32_t n,
                                 uint32_t bits, void* stream);
 
+/* The same sort for callers that may not allocate device memory when they
+ * sort (a pool allocator that owns the device, an allocation-free section
+ * of a stream, a plugin handed only its buffers).  No counterpart in the
+ * reference.  Needs no handle: its scratch is a fixed static device array,
+ * so it makes no cudaMalloc/cudaFree call and calls no allocating library.
+ *   - n is at most GSAP_NOALLOC_SORT_MAX_N; larger n returns
+ *     GSAP_ERR_CAPACITY before any work is queued.
+ *   - The first call on each device does the set-up (looks up the array,
+ *     zeroes its control block and look-back words, synchronises the
+ *     device); make it before any stream capture begins.
+ *   - One scratch per device: calls that overlap in time (other streams,
+ *     other host threads) race.  Serialise them.
+ *   - d_vals may be NULL (keys only).  Synchronises `stream` to read the
+ *     device error word. */
+#define GSAP_NOALLOC_SORT_MAX_N (1u << 20)
+gsap_status gsap_radix_sort_u32_noalloc(uint32_t* d_keys, uint32_t* d_vals, uint32_t n, uint32_t bits,
+                                        void* stream);
+
 /* ----------------------------------------------------------- rigid bodies */
 
 typedef struct gsap_rb gsap_rb;
