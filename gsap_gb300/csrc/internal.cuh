@@ -92,7 +92,8 @@ struct BpScratch {
     uint64_t* status;          // look-back words (per tile and digit)
     float4* smin;              // sweep entries in sorted order: bounds (sphere in smin)
     float4* smax;
-    uint32_t* scell;           // sorted entries: (c2lo << 16) | c3lo of the object
+    uint8_t* sflag;            // sorted entries: owner flags (bit 0: the entry's cell column is the
+                               // object's lowest on u2, bit 1: its row is the lowest on u3)
     uint32_t* longrows;        // canonical output: ids of rows longer than 32
     uint32_t* rowcnt;          // per object pair counts (canonical output)
     uint32_t* rowoff;          // exclusive offsets, n+1
@@ -124,15 +125,17 @@ struct BpArgs {
 cudaError_t launch_plan(const BpScratch& s, const BpArgs& a, cudaStream_t st);
 cudaError_t launch_pca(const BpScratch& s, const BpArgs& a, cudaStream_t st);
 cudaError_t launch_project(const BpScratch& s, const BpArgs& a, int passes, cudaStream_t st);
-// Gather epilogue of the last sort pass: entry g also gets the bounds and
-// lower-corner cell of its object, so the sweep reads candidates in order.
+// Gather epilogue of the last sort pass: entry g also gets the bounds of its
+// object and its owner flags, so the sweep reads candidates in order.
 struct SortGather {
     const float4* mn;
     const float4* mx;          // nullptr in sphere mode
     const uint32_t* objcell;
+    const uint32_t* objscene;  // nullptr for one scene
+    const Scene* scenes;
     float4* smin;
     float4* smax;
-    uint32_t* scell;
+    uint8_t* sflag;
 };
 cudaError_t launch_sort_pass(const BpScratch& s, int pass, int passes, const uint32_t* kin,
                              const uint32_t* vin, uint32_t* kout, uint32_t* vout,

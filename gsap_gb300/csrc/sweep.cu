@@ -9,23 +9,29 @@
 // and the cross pass of SapKernel.cu:2364-2446.
 //
 // Persistent warps take 32 consecutive sorted entries at a time from an
-// atomic counter (work stealing).  Each lane scans forward from its entry,
-// kUnroll candidates per iteration with their loads issued together,
-// while the candidate key is <= (bucket | q(hi1)): the q map is monotone, so
-// every later entry of the same cell whose interval on u1 can meet this one
-// is visited, and the scan stops at the cell (and scene) boundary by
-// construction.  The last sort pass wrote every entry's bounds and
-// lower-corner cell in sorted order, so lane L at step k reads entry
-// e + L + k: the 32 lanes read one contiguous run and the next step re-reads
-// it shifted by one (L1 hits) -- no random gathers in the hot loop.
+// atomic counter (work stealing).  For its entry e a lane first finds, by a
+// galloping then binary search over the sorted keys, the end of the run of
+// entries with key <= (bucket | q(hi1)): the q map is monotone, so these are
+// exactly the later entries of the same cell whose interval on u1 can meet
+// e's, and the run stops at the cell (and scene) boundary by construction.
+// The warp then flattens the 32 runs into one list of candidate tests (a
+// warp scan of the run lengths) and works through it 32 tests per step, test
+// t on lane t mod 32: every lane does useful work however uneven the runs
+// are, and the lanes of a step read consecutive candidates (coalesced; the
+// last sort pass wrote every entry's bounds in sorted order).  A lane finds
+// the entry of its test from the run starts that fall into the step's
+// window (one warp OR-reduction and a popcount) and reads that entry's
+// bounds from shared memory.
 // Candidates pass the exact test on the original FP32 bounds (closed AABB
 // test of Aabb::overlaps, include/aabb.h:47-57, or the strict squared
 // sphere test of SapKernel.cu:1897-1903 with one rounding per operation)
 // and the owner-cell rule: a pair is reported only in the cell holding
 // (max(lo2_i, lo2_j), max(lo3_i, lo3_j)), which both objects touch, so each
 // overlapping pair comes out exactly once and no sort + unique pass is
-// needed.  Hits are compacted through a per-warp shared-memory buffer that
-// reserves global space with one atomic per up to 128 pairs.
+// needed.  With the per-entry owner flags of the gather (is this cell the
+// object's lowest on u2 / on u3) the rule is (f_i | f_j) == 3.  Hits are
+// compacted through a per-warp shared-memory buffer that reserves global
+// space with one atomic per up to 128 pairs.
 #include "internal.cuh"
 
 namespace gsap {
@@ -38,25 +44,33 @@ __device__ __forceinline__ float proj_hi(const float* u, float3 a, float3 b) {
 }
 
 constexpr int kBuf = 128;  // pairs buffered per warp before a global reservation
-constexpr int kUnroll = 4; // candidates per lane per iteration (loads issued together)
+constexpr int kWarps = kThreads / 32;
 
 template <int MODE>
 __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const uint32_t* __restrict__ keys,
                                                     const uint32_t* __restrict__ vals, uint2* __restrict__ pairs,
                                                     uint64_t pair_cap, int count_rows) {
-    __shared__ uint2 s_buf[kThreads / 32][kBuf];
+    __shared__ uint2 s_buf[kWarps][kBuf];
+    // entries of the warp's chunk that have candidates, in run order
+    __shared__ float4 s_pa[kWarps][32];
+    __shared__ float4 s_pb[kWarps][MODE == 0 ? 32 : 1];
+    __shared__ uint32_t s_id[kWarps][32];  // object index
+    __shared__ uint32_t s_jb[kWarps][32];  // candidate of test t is s_jb + t
+    __shared__ uint32_t s_fl[kWarps][32];  // owner flags
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const uint32_t lt = lanemask_lt();
+    const uint32_t le = lt | (1u << lane);
     Ctrl* C = S.ctrl;
     const float4* __restrict__ smin = S.smin;
     const float4* __restrict__ smax = S.smax;
-    const uint32_t* __restrict__ scell = S.scell;
+    const uint8_t* __restrict__ sflag = S.sflag;
     const uint32_t E = (uint32_t)min((uint64_t)C->entry_count, S.entry_cap);
     const uint32_t Q = C->qbits;
     const uint32_t qmask = (1u << Q) - 1u;
     const float qmax = (float)qmask;
     uint32_t nbuf = 0;
-    uint32_t my_tests = 0, iters = 0;
+    uint64_t tests = 0;
+    uint32_t steps = 0;
 
     auto flush = [&]() {
         __syncwarp();
@@ -83,10 +97,10 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= E) break;
         const uint32_t e = base + lane;
-        bool live = e < E;
-        uint32_t i = 0, kb = 0, bucket = 0, ci = 0, bbase = 0, g3 = 1;
+        uint32_t run = 0;  // candidates of entry e: e+1 .. e+run
         float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), pb = pa;
-        if (live) {
+        uint32_t i = 0;
+        if (e < E) {
             const uint32_t key = keys[e];
             i = vals[e];
             const Scene* sc = &S.scenes[S.objscene ? S.objscene[i] : 0u];
@@ -105,79 +119,90 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
             float h1 = proj_hi(u, a, b);
             float t = __fmul_rn(__fsub_rn(h1, sc->q_org), sc->q_scale);
             uint32_t qh = (uint32_t)fminf(fmaxf(t, 0.f), qmax);
-            kb = (key & ~qmask) | qh;
-            bucket = key >> Q;
-            bbase = sc->bucket_base;
-            g3 = sc->G3;
-            ci = scell[e];
-        }
-        uint32_t j = e + 1;
-        while (true) {
-            // the next kUnroll candidates: keys are sorted, so the active ones form a prefix
-            bool act[kUnroll];
-#pragma unroll
-            for (int u = 0; u < kUnroll; ++u) {
-                const uint32_t jj = j + u;
-                act[u] = live && jj < E && __ldg(keys + jj) <= kb;
+            const uint32_t kb = (key & ~qmask) | qh;  // >= key: q(hi1) >= q(lo1)
+            // last index with key <= kb: gallop from e, then bisect (lo: key <= kb, hi: key > kb or E)
+            uint32_t lo = e, hi = E, step = 1;
+            while (true) {
+                if (step >= E - lo) break;
+                const uint32_t p = lo + step;
+                if (__ldg(keys + p) > kb) { hi = p; break; }
+                lo = p;
+                step <<= 1;
             }
+            while (hi - lo > 1) {
+                const uint32_t mid = lo + ((hi - lo) >> 1);
+                if (__ldg(keys + mid) <= kb) lo = mid;
+                else hi = mid;
+            }
+            run = lo - e;
+        }
+        // flatten the runs: exclusive start of each run in the warp's test list
+        uint32_t x = run;
 #pragma unroll
-            for (int u = 1; u < kUnroll; ++u) act[u] = act[u] && act[u - 1];
-            if (!__any_sync(0xffffffffu, act[0])) break;
-            ++iters;
-            float4 qa[kUnroll], qb[kUnroll];
-#pragma unroll
-            for (int u = 0; u < kUnroll; ++u)
-                if (act[u]) {
-                    qa[u] = __ldg(smin + j + u);
-                    if (MODE == 0) qb[u] = __ldg(smax + j + u);
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, x, 31);
+        const uint32_t start = x - run;
+        const uint32_t nz = __ballot_sync(0xffffffffu, run > 0);
+        if (run > 0) {
+            const uint32_t r = __popc(nz & lt);
+            s_pa[wid][r] = pa;
+            if (MODE == 0) s_pb[wid][r] = pb;
+            s_id[wid][r] = i;
+            s_jb[wid][r] = e + 1u - start;
+            s_fl[wid][r] = sflag[e];
+        }
+        __syncwarp();
+        tests += total;
+        uint32_t before = 0;  // runs that start before the current window
+        for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+            ++steps;
+            const uint32_t d = start - t0;
+            const uint32_t starts = __reduce_or_sync(0xffffffffu, (run > 0 && d < 32u) ? (1u << d) : 0u);
+            const uint32_t t = t0 + lane;
+            bool hit = false;
+            uint32_t o = 0, oi = 0;
+            if (t < total) {
+                const uint32_t m = before + __popc(starts & le) - 1u;  // run of test t
+                const uint32_t j = s_jb[wid][m] + t;
+                const float4 ea = s_pa[wid][m];
+                const float4 qa = __ldg(smin + j);
+                bool ov;
+                if (MODE == 0) {
+                    const float4 eb = s_pb[wid][m];
+                    const float4 qb = __ldg(smax + j);
+                    ov = (ea.x <= qb.x) & (qa.x <= eb.x) & (ea.y <= qb.y) & (qa.y <= eb.y) & (ea.z <= qb.z) &
+                         (qa.z <= eb.z);
+                } else {
+                    float dx = __fsub_rn(ea.x, qa.x), dy = __fsub_rn(ea.y, qa.y), dz = __fsub_rn(ea.z, qa.z);
+                    float t1 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                    float rr = __fadd_rn(ea.w, qa.w);
+                    ov = t1 < __fmul_rn(rr, rr);
                 }
-#pragma unroll
-            for (int u = 0; u < kUnroll; ++u) {
-                bool hit = false;
-                uint32_t o = 0;
-                if (act[u]) {
-                    ++my_tests;
-                    bool ov;
-                    if (MODE == 0) {
-                        ov = (pa.x <= qb[u].x) & (qa[u].x <= pb.x) & (pa.y <= qb[u].y) & (qa[u].y <= pb.y) &
-                             (pa.z <= qb[u].z) & (qa[u].z <= pb.z);
-                    } else {
-                        float dx = __fsub_rn(pa.x, qa[u].x), dy = __fsub_rn(pa.y, qa[u].y),
-                              dz = __fsub_rn(pa.z, qa[u].z);
-                        float t1 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-                        float r = __fadd_rn(pa.w, qa[u].w);
-                        ov = t1 < __fmul_rn(r, r);
-                    }
-                    if (ov) {
-                        // owner-cell rule: the pair belongs to the cell of (max lo2, max lo3)
-                        const uint32_t co = __ldg(scell + j + u);
-                        const uint32_t own = bbase + max(ci >> 16, co >> 16) * g3 + max(ci & 0xFFFFu, co & 0xFFFFu);
-                        if (own == bucket) {
-                            hit = true;
-                            o = __ldg(vals + j + u);
-                        }
-                    }
-                }
-                const uint32_t hm = __ballot_sync(0xffffffffu, hit);
-                if (hm) {
-                    const uint32_t cnt = __popc(hm);
-                    if (nbuf + cnt > kBuf) flush();
-                    if (hit) s_buf[wid][nbuf + __popc(hm & lt)] = make_uint2(min(i, o), max(i, o));
-                    nbuf += cnt;
+                if (ov && (s_fl[wid][m] | __ldg(sflag + j)) == 3u) {
+                    hit = true;
+                    o = __ldg(vals + j);
+                    oi = s_id[wid][m];
                 }
             }
-            live = act[kUnroll - 1];
-            j += kUnroll;
+            before += __popc(starts);
+            const uint32_t hm = __ballot_sync(0xffffffffu, hit);
+            if (hm) {
+                const uint32_t cnt = __popc(hm);
+                if (nbuf + cnt > kBuf) flush();
+                if (hit) s_buf[wid][nbuf + __popc(hm & lt)] = make_uint2(min(oi, o), max(oi, o));
+                nbuf += cnt;
+            }
         }
+        __syncwarp();  // the next chunk overwrites the run table
     }
     flush();
-    // diagnostics: candidate tests and warp iterations of this warp
-    uint32_t t = my_tests;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
-    if (lane == 0 && t) {
-        atomicAdd(&C->tests, (unsigned long long)t);
-        atomicAdd(&C->iters, (unsigned long long)iters);
+    // diagnostics: candidate tests and warp steps
+    if (lane == 0 && tests) {
+        atomicAdd(&C->tests, (unsigned long long)tests);
+        atomicAdd(&C->iters, (unsigned long long)steps);
     }
 }
 
