@@ -111,7 +111,7 @@ static void free_scratch(gsap_sap* h) {
     BpScratch& s = h->s;
     void* ptrs[] = {s.ctrl, s.scenes, s.partials, s.scene_done, s.work_start, s.objcell, s.objscene,
                     s.keys[0], s.keys[1], s.vals[0], s.vals[1], s.status, s.rowcnt, s.rowoff, s.tmp_pairs,
-                    s.smin, s.smax, s.sflag, s.longrows};
+                    s.smin, s.smax, s.longrows};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (h->h_ctrl) cudaFreeHost(h->h_ctrl);
@@ -172,7 +172,6 @@ extern "C" gsap_sap* gsap_sap_create(uint32_t max_n, const gsap_config* cfg) {
     A((void**)&s.status, 8ull * s.status_words);
     A((void**)&s.smin, 16ull * ecap);
     A((void**)&s.smax, 16ull * ecap);
-    A((void**)&s.sflag, ecap);
     A((void**)&s.longrows, 4ull * (max_n + 1));
     A((void**)&s.rowcnt, 4ull * (max_n + 1));
     A((void**)&s.rowoff, 4ull * (max_n + 1));
@@ -252,7 +251,7 @@ static gsap_status record(gsap_sap* h, const Call& c, cudaStream_t st, bool time
     const uint32_t* count = &s.ctrl->entry_count;
     int src = 0;
     SortGather gather{c.mn, c.mode == GSAP_MODE_AABB ? c.mx : nullptr, s.objcell, s.objscene, s.scenes,
-                      s.smin, s.smax, s.sflag};
+                      s.smin, s.smax};
     for (int p = 0; p < passes; ++p) {
         CK(launch_sort_pass(s, p, passes, s.keys[src], s.vals[src], s.keys[src ^ 1], s.vals[src ^ 1], count,
                             s.entry_cap, a.spin_limit, st, p == passes - 1 ? &gather : nullptr, true));

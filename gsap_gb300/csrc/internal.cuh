@@ -90,10 +90,13 @@ struct BpScratch {
     uint32_t* keys[2];
     uint32_t* vals[2];
     uint64_t* status;          // look-back words (per tile and digit)
-    float4* smin;              // sweep entries in sorted order: bounds (sphere in smin)
+    // Sweep entries in sorted order, one 32-byte record each.  Boxes:
+    // smin = (lo.xyz, object index bits), smax = (hi.xyz, owner flag bits).
+    // Spheres: smin = (centre.xyz, radius), smax = (object index bits, owner
+    // flag bits, 0, 0).  Owner flags: bit 0 when the entry's cell column is
+    // the object's lowest on u2, bit 1 when its row is the lowest on u3.
+    float4* smin;
     float4* smax;
-    uint8_t* sflag;            // sorted entries: owner flags (bit 0: the entry's cell column is the
-                               // object's lowest on u2, bit 1: its row is the lowest on u3)
     uint32_t* longrows;        // canonical output: ids of rows longer than 32
     uint32_t* rowcnt;          // per object pair counts (canonical output)
     uint32_t* rowoff;          // exclusive offsets, n+1
@@ -135,7 +138,6 @@ struct SortGather {
     const Scene* scenes;
     float4* smin;
     float4* smax;
-    uint8_t* sflag;
 };
 cudaError_t launch_sort_pass(const BpScratch& s, int pass, int passes, const uint32_t* kin,
                              const uint32_t* vin, uint32_t* kout, uint32_t* vout,

@@ -29,7 +29,9 @@
 // (max(lo2_i, lo2_j), max(lo3_i, lo3_j)), which both objects touch, so each
 // overlapping pair comes out exactly once and no sort + unique pass is
 // needed.  With the per-entry owner flags of the gather (is this cell the
-// object's lowest on u2 / on u3) the rule is (f_i | f_j) == 3.  Hits are
+// object's lowest on u2 / on u3) the rule is (f_i | f_j) == 3.  Object index
+// and flags travel inside the two 16-byte bound records, so a test makes
+// no load that depends on another.  Hits are
 // compacted through a per-warp shared-memory buffer that reserves global
 // space with one atomic per up to 128 pairs.
 #include "internal.cuh"
@@ -63,7 +65,6 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
     Ctrl* C = S.ctrl;
     const float4* __restrict__ smin = S.smin;
     const float4* __restrict__ smax = S.smax;
-    const uint8_t* __restrict__ sflag = S.sflag;
     const uint32_t E = (uint32_t)min((uint64_t)C->entry_count, S.entry_cap);
     const uint32_t Q = C->qbits;
     const uint32_t qmask = (1u << Q) - 1u;
@@ -100,14 +101,16 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
         uint32_t run = 0;  // candidates of entry e: e+1 .. e+run
         float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), pb = pa;
         uint32_t i = 0;
+        uint32_t fl = 0;
         if (e < E) {
             const uint32_t key = keys[e];
-            i = vals[e];
-            const Scene* sc = &S.scenes[S.objscene ? S.objscene[i] : 0u];
             pa = smin[e];
+            pb = smax[e];
+            i = __float_as_uint(MODE == 0 ? pa.w : pb.x);
+            fl = __float_as_uint(MODE == 0 ? pb.w : pb.y);
+            const Scene* sc = &S.scenes[S.objscene ? S.objscene[i] : 0u];
             float3 a, b;
             if (MODE == 0) {
-                pb = smax[e];
                 a = make_float3(pa.x, pa.y, pa.z);
                 b = make_float3(pb.x, pb.y, pb.z);
             } else {
@@ -152,7 +155,7 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
             if (MODE == 0) s_pb[wid][r] = pb;
             s_id[wid][r] = i;
             s_jb[wid][r] = e + 1u - start;
-            s_fl[wid][r] = sflag[e];
+            s_fl[wid][r] = fl;
         }
         __syncwarp();
         tests += total;
@@ -170,20 +173,26 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
                 const float4 ea = s_pa[wid][m];
                 const float4 qa = __ldg(smin + j);
                 bool ov;
+                uint32_t jid, jfl;
                 if (MODE == 0) {
                     const float4 eb = s_pb[wid][m];
                     const float4 qb = __ldg(smax + j);
+                    jid = __float_as_uint(qa.w);
+                    jfl = __float_as_uint(qb.w);
                     ov = (ea.x <= qb.x) & (qa.x <= eb.x) & (ea.y <= qb.y) & (qa.y <= eb.y) & (ea.z <= qb.z) &
                          (qa.z <= eb.z);
                 } else {
+                    const uint2 w = __ldg(reinterpret_cast<const uint2*>(smax + j));
+                    jid = w.x;
+                    jfl = w.y;
                     float dx = __fsub_rn(ea.x, qa.x), dy = __fsub_rn(ea.y, qa.y), dz = __fsub_rn(ea.z, qa.z);
                     float t1 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
                     float rr = __fadd_rn(ea.w, qa.w);
                     ov = t1 < __fmul_rn(rr, rr);
                 }
-                if (ov && (s_fl[wid][m] | __ldg(sflag + j)) == 3u) {
+                if (ov && (s_fl[wid][m] | jfl) == 3u) {
                     hit = true;
-                    o = __ldg(vals + j);
+                    o = jid;
                     oi = s_id[wid][m];
                 }
             }
