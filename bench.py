@@ -169,11 +169,15 @@ def run_ours(args, world, rank, local):
     n = args.n
     host_sets, R = make_inputs(rank, n, args.jitter_sets)
     dsets = [(torch.from_numpy(mn).to(dev), torch.from_numpy(mx).to(dev)) for mn, mx in host_sets]
-    sap = Sap(n, cell_factor=args.cell_factor, sort_bits=args.sort_bits)
+    fixed = args.cell_factor is not None or args.sort_bits is not None or args.no_tune
+    sap = Sap(n, cell_factor=args.cell_factor or 2.0, sort_bits=args.sort_bits or 32)
     cap = 16 * n
     pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
     d_count = torch.zeros(1, dtype=torch.int64, device=dev)
     stream = torch.cuda.current_stream()
+    # autotuner (set-up, untimed): key width and cell factor for this input
+    tuned = None if fixed else sap.autotune(*dsets[0], pairs=pairs, sorted=True, graph=True, reps=3, stream=stream)
+    passes = (tuned["sort_bits"] if tuned else (args.sort_bits or 32)) // 8
 
     def call(k, sorted_=True, graph=True):
         mn, mx = dsets[k % len(dsets)]
@@ -231,7 +235,7 @@ def run_ours(args, world, rank, local):
     pipe_gbs = alg["total"] / (ms / 1e3) / 1e9
 
     # unsorted pair set (no canonicalisation), for reference
-    for k in range(3):
+    for k in range(16):
         call(k, sorted_=False)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -283,7 +287,8 @@ def run_ours(args, world, rank, local):
     if not args.no_extras:
         extras = run_extras(args, dev, stream)
 
-    launches_per_call = 10  # pca, project, 4 sort passes, sweep, scan, scatter, row sort
+    # pca + finish, project, one per radix pass, sweep, scan, scatter, row sort (short and long rows)
+    launches_per_call = 8 + passes
     clocks = clk.summary()
     line = {
         "metric": "1M-AABB PCA sweep-and-prune broadphase throughput (sorted i<j pair set)",
@@ -294,7 +299,9 @@ def run_ours(args, world, rank, local):
                                "rotation, log-normal half-extents, 64 jittered copies cycled",
                    "n": n, "pairs_per_call": P0,
                    "l2": f"inputs cycled over {len(dsets)} x {2 * n * 16 >> 20} MiB",
-                   "output": "sorted (i<j) uint32 pairs", "parallelism": f"replicas x{world}"},
+                   "output": "sorted (i<j) uint32 pairs", "parallelism": f"replicas x{world}",
+                   "settings": dict(tuned, autotuned=True) if tuned else
+                   {"sort_bits": args.sort_bits or 32, "cell_factor": args.cell_factor or 2.0, "autotuned": False}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": f"stage:{dom}",
                      "peak_kind": peak_kind},
@@ -459,7 +466,7 @@ def run_reference(args, world, rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=64)
+    ap.add_argument("--steps", type=int, default=1024)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_OBJ)
@@ -467,8 +474,10 @@ def main():
     ap.add_argument("--bodies", type=int, default=65536)
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cell-factor", type=float, default=1.5, help="sweep cell size / mean projected width")
-    ap.add_argument("--sort-bits", type=int, default=32, choices=[24, 32])
+    ap.add_argument("--cell-factor", type=float, default=None,
+                    help="sweep cell size / mean projected width (default: autotuned)")
+    ap.add_argument("--sort-bits", type=int, default=None, choices=[24, 32], help="radix key width (default: autotuned)")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (defaults: 32 bits, cell factor 2.0)")
     ap.add_argument("--jitter-sets", type=int, default=N_JITTER,
                     help="distinct jittered inputs cycled by the timed calls (64 = the workload)")
     args = ap.parse_args()

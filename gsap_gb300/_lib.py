@@ -62,6 +62,7 @@ SIGNATURES = [
     ("gsap_sap_scene_axes", I32, [P, U32, C.POINTER(F64), P]),
     ("gsap_sap_stage_times", C.c_int, [P, C.POINTER(F32), C.c_int]),
     ("gsap_sap_enable_timing", None, [P, C.c_int]),
+    ("gsap_sap_autotune", I32, [P, P, P, P, U32, U32, P, U64, U32, C.c_int, C.POINTER(Config), P]),
     ("gsap_radix_sort_u32", I32, [P, P, P, U32, U32, P]),
     ("gsap_radix_sort_u32_noalloc", I32, [P, P, U32, U32, P]),
     ("gsap_rb_create", P, [I32, I32, I32]),

@@ -73,7 +73,7 @@ extern "C" void gsap_config_default(gsap_config* c) {
     c->entry_factor = 8;
     c->pair_factor = 16;
     c->sort_bits = 32;
-    c->cell_factor = 1.5f;
+    c->cell_factor = 2.0f;
     c->spin_limit = kDefaultSpin;
 }
 
@@ -82,6 +82,8 @@ extern "C" void gsap_config_default(gsap_config* c) {
 struct GraphKey {
     const void *mn, *mx, *off, *pairs, *dcount, *entries;
     uint32_t n, S, flags, mode, both;
+    uint32_t key_bits;
+    float cell_factor;
     uint64_t cap, ecap;
     bool operator==(const GraphKey& o) const { return memcmp(this, &o, sizeof(*this)) == 0; }
 };
@@ -134,7 +136,7 @@ extern "C" gsap_sap* gsap_sap_create(uint32_t max_n, const gsap_config* cfg) {
     if (c.pair_factor == 0) c.pair_factor = 16;
     if (c.sort_bits == 0) c.sort_bits = 32;
     if (c.sort_bits != 24 && c.sort_bits != 32) { fail(GSAP_ERR_INVALID, "sort_bits must be 24 or 32"); return nullptr; }
-    if (c.cell_factor <= 0.f) c.cell_factor = 1.5f;
+    if (c.cell_factor <= 0.f) c.cell_factor = 2.0f;
     if (c.spin_limit == 0) c.spin_limit = kDefaultSpin;
     if (max_n == 0) max_n = 1;
     uint64_t ecap = (uint64_t)c.entry_factor * max_n + 4096;
@@ -284,6 +286,7 @@ static gsap_status run(gsap_sap* h, const Call& c, cudaStream_t st) {
     k.mn = c.mn; k.mx = c.mx; k.off = c.off; k.pairs = c.pairs; k.dcount = c.d_count; k.entries = c.entries;
     k.n = c.n; k.S = c.S; k.flags = c.flags; k.mode = (uint32_t)c.mode; k.both = (uint32_t)c.both;
     k.cap = c.cap; k.ecap = c.ecap;
+    k.key_bits = h->cfg.sort_bits; k.cell_factor = h->cfg.cell_factor;  // tuned settings are baked into a graph
     // LRU cache of captured pipelines, one per (inputs, outputs, sizes, flags)
     GraphEntry* hit = nullptr;
     for (auto& g : *h->graphs)
@@ -391,6 +394,60 @@ extern "C" gsap_status gsap_broadphase_aabb(gsap_sap* h, const float* d_min, con
                                             uint32_t* d_pairs, uint64_t pair_cap, uint64_t* d_count,
                                             uint64_t* h_count, uint32_t flags, void* stream) {
     return broadphase(h, d_min, d_max, nullptr, 1, n, d_pairs, pair_cap, d_count, h_count, flags, stream);
+}
+
+// Times every (key width, cell factor) pair of a small grid on the caller's
+// input and keeps the fastest in the handle.  Key width sets the radix
+// passes (24 bits: three 8-bit digits, 32 bits: four) and the q resolution
+// of the sweep; the cell factor sets the cell edge on u2/u3 and with it the
+// replication (entries to sort) against the candidate run length (tests).
+// Any setting gives the same pair set; only the time differs.
+extern "C" gsap_status gsap_sap_autotune(gsap_sap* h, const float* d_min, const float* d_max,
+                                         const uint32_t* d_scene_offsets, uint32_t num_scenes, uint32_t n,
+                                         uint32_t* d_pairs, uint64_t pair_cap, uint32_t flags, int reps,
+                                         gsap_config* out, void* stream) {
+    if (!h) return fail(GSAP_ERR_INVALID, "null handle");
+    if (reps < 1) reps = 1;
+    if (d_scene_offsets && num_scenes == 0) return fail(GSAP_ERR_INVALID, "batched call needs scene offsets");
+    const uint32_t S = d_scene_offsets ? num_scenes : 1;
+    const uint32_t bits_grid[2] = {24, 32};
+    const float cf_grid[5] = {1.0f, 1.5f, 2.0f, 2.5f, 3.0f};
+    const gsap_config saved = h->cfg;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best_ms = -1.f;
+    gsap_config best = saved;
+    for (uint32_t bits : bits_grid)
+        for (float cf : cf_grid) {
+            h->cfg.sort_bits = bits;
+            h->cfg.cell_factor = cf;
+            uint64_t cnt = 0;
+            // untimed first call: builds the graph and checks capacities
+            gsap_status r = broadphase(h, d_min, d_max, d_scene_offsets, S, n, d_pairs, pair_cap, nullptr, &cnt,
+                                       flags, stream);
+            if (r != GSAP_OK) continue;  // this setting does not fit the handle; try the next
+            cudaEventRecord(e0, st);
+            for (int k = 0; k < reps && r == GSAP_OK; ++k)
+                r = broadphase(h, d_min, d_max, d_scene_offsets, S, n, d_pairs, pair_cap, nullptr, nullptr, flags,
+                               stream);
+            cudaEventRecord(e1, st);
+            if (r == GSAP_OK) r = finish(h, st, &cnt, ~0ull);
+            float ms = 0.f;
+            if (r != GSAP_OK || cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+                continue;
+            if (best_ms < 0.f || ms < best_ms) {
+                best_ms = ms;
+                best = h->cfg;
+            }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    h->cfg = best;
+    if (best_ms < 0.f) return fail(GSAP_ERR_CAPACITY, "no setting of the tuning grid fits this input");
+    if (out) *out = best;
+    return GSAP_OK;
 }
 
 extern "C" gsap_status gsap_broadphase_batched(gsap_sap* h, const float* d_min, const float* d_max,

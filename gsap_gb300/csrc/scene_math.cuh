@@ -208,7 +208,7 @@ __host__ __device__ inline void choose_scene(const SceneSums& z, const BpArgs& A
     if (!(r2 > 1e-30f) || !isfinite(r2)) r2 = 1.f;
     if (!(r3 > 1e-30f) || !isfinite(r3)) r3 = 1.f;
     const float width = hw[1] + hw[2];  // mean full width averaged over the two axes
-    const float cf = A.cell_factor > 0 ? A.cell_factor : 1.5f;
+    const float cf = A.cell_factor > 0 ? A.cell_factor : 2.0f;
     const float target = 16.f;           // aim for at least this many objects per cell
     float s = cf * width;
     float sd = sqrtf(r2 * r3 * target / (nf > 1.f ? nf : 1.f));

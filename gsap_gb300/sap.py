@@ -59,7 +59,7 @@ class Sap:
     """GB300 sweep-and-prune broadphase handle (owns all scratch)."""
 
     def __init__(self, max_n: int, mode: int = MODE_AABB, axis_mode: int = AXIS_PCA, max_scenes: int = 1,
-                 entry_factor: int = 8, pair_factor: int = 16, sort_bits: int = 32, cell_factor: float = 1.5,
+                 entry_factor: int = 8, pair_factor: int = 16, sort_bits: int = 32, cell_factor: float = 2.0,
                  spin_limit: int = 0):
         L = load()
         cfg = Config()
@@ -136,6 +136,28 @@ class Sap:
             return pairs[: cnt.value]
         check(st)
         return pairs[: cnt.value]
+
+    def autotune(self, mn: torch.Tensor, mx: torch.Tensor | None = None, offsets: torch.Tensor | None = None,
+                 pairs: torch.Tensor | None = None, sorted: bool = True, graph: bool = True, reps: int = 3,
+                 stream=None) -> dict:
+        """Picks key width and cell factor for this kind of input by timing a
+        small grid on it (gsap_sap_autotune); the handle keeps the fastest.
+        Returns the chosen settings."""
+        n = mn.shape[0]
+        _dev_ptr(mn, "mn", torch.float32, 4)
+        _dev_ptr(mx, "mx", torch.float32, 4)
+        _dev_ptr(offsets, "offsets", torch.int32)
+        flags = (FLAG_SORTED if sorted else 0) | (FLAG_GRAPH if graph else 0)
+        if pairs is None:
+            pairs = torch.empty((max(16, 8 * n), 2), dtype=torch.int32, device=mn.device)
+        cfg = Config()
+        S = offsets.numel() - 1 if offsets is not None else 0
+        check(load().gsap_sap_autotune(self._h, mn.data_ptr(), mx.data_ptr() if mx is not None else None,
+                                       offsets.data_ptr() if offsets is not None else None, C.c_uint32(S),
+                                       C.c_uint32(n), pairs.data_ptr(), C.c_uint64(pairs.shape[0]),
+                                       C.c_uint32(flags), C.c_int(reps), C.byref(cfg),
+                                       C.c_void_p(_stream_ptr(stream))))
+        return {"sort_bits": int(cfg.sort_bits), "cell_factor": float(cfg.cell_factor)}
 
     def broadphase_async(self, mn, mx, pairs, d_count, sorted=False, graph=False, stream=None):
         """Asynchronous form: the pair count goes to the device tensor

@@ -69,7 +69,7 @@ typedef struct gsap_config {
     uint32_t entry_factor;  /* sweep-entry capacity = entry_factor * max_n (0 -> 8) */
     uint32_t pair_factor;   /* internal pair capacity = pair_factor * max_n (0 -> 16) */
     uint32_t sort_bits;     /* radix key width, 24 or 32 (0 -> 32) */
-    float cell_factor;      /* cell size / mean projected width on the secondary axes (0 -> 1.5) */
+    float cell_factor;      /* cell size / mean projected width on the secondary axes (0 -> 2.0) */
     uint32_t spin_limit;    /* iteration cap of every device-side wait (0 -> default) */
 } gsap_config;
 
@@ -146,6 +146,21 @@ gsap_status gsap_sap_scene_axes(gsap_sap* h, uint32_t scene, double* out, void* 
  * of stages written. */
 int gsap_sap_stage_times(gsap_sap* h, float* out_ms, int max_stages);
 void gsap_sap_enable_timing(gsap_sap* h, int enable);
+
+/* Autotuner: runs the broadphase on the given input (single scene when
+ * d_scene_offsets is NULL, else batched) for every setting of a small grid
+ * -- key width 24/32 bits (three or four radix passes) x cell factor
+ * 1.0/1.5/2.0/2.5/3.0 (the u2/u3 cell edge, which trades sort volume
+ * against sweep run length) -- times `reps` calls of each with CUDA events
+ * on `stream`, and keeps the fastest setting in the handle (written to *out
+ * if non-NULL).  d_pairs/pair_cap are used as output scratch.  Settings
+ * that overflow the handle's capacities are skipped.  Any setting yields
+ * the same pair set.  Synchronises `stream`.  No reference counterpart
+ * (the reference reuses a fixed interval between frames, Sap.cpp:226-243). */
+gsap_status gsap_sap_autotune(gsap_sap* h, const float* d_min, const float* d_max,
+                              const uint32_t* d_scene_offsets, uint32_t num_scenes, uint32_t n,
+                              uint32_t* d_pairs, uint64_t pair_cap, uint32_t flags, int reps,
+                              gsap_config* out, void* stream);
 
 /* Stable LSD radix sort of n (key, value) uint32 pairs on the low `bits`
  * bits with the onesweep kernels of the broadphase (decoupled look-back,

@@ -39,7 +39,7 @@ def test_config_defaults(gsap_lib):
     c = Config()
     gsap_lib.gsap_config_default(C.byref(c))
     assert (c.mode, c.axis_mode, c.max_scenes, c.entry_factor, c.sort_bits) == (0, 0, 1, 8, 32)
-    assert abs(c.cell_factor - 1.5) < 1e-7
+    assert abs(c.cell_factor - 2.0) < 1e-7
 
 
 def test_struct_sizes(gsap_lib):

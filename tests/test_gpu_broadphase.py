@@ -156,3 +156,33 @@ def test_gauss_1m_against_cpu_sap(cuda, oracle_lib, axis_mode):
     if axis_mode == 0:
         ax = np.array(sap.scene_axes()["axes"][0])
         assert abs(abs(ax @ R[:, 0]) - 1.0) < 1e-3
+
+
+def test_autotune_keeps_the_pair_set(cuda, oracle_lib):
+    """Every setting of the tuning grid gives the same pair set; the tuner's
+    choice lies in the grid and the handle keeps using it."""
+    import torch
+    from gsap_gb300 import Sap, scenes
+    n = 60_000
+    c, h, _ = scenes.aabb_gauss_parts(n, seed=11, std=(30.0, 8.0, 2.0))
+    mn = np.concatenate([c - h, np.zeros((n, 1), np.float32)], 1)
+    mx = np.concatenate([c + h, np.zeros((n, 1), np.float32)], 1)
+    want = oracle_lib.bf_aabb(mn, mx)
+    sap = Sap(n)
+    dmn, dmx = to_dev(mn, cuda), to_dev(mx, cuda)
+    cfg = sap.autotune(dmn, dmx, reps=2)
+    assert cfg["sort_bits"] in (24, 32) and cfg["cell_factor"] in (1.0, 1.5, 2.0, 2.5, 3.0)
+    for graph in (False, True):
+        got = sap.broadphase(dmn, dmx, sorted=True, graph=graph).cpu().numpy().astype(np.uint32)
+        assert np.array_equal(got, want)
+    # batched form of the tuner
+    mnb, mxb, off = scenes.batched_aabb(S=24, seed=5, lo=16, hi=3000)
+    bsap = Sap(len(mnb), max_scenes=24)
+    doff = torch.from_numpy(off.astype(np.int32)).to(cuda)
+    bm, bx = to_dev(mnb, cuda), to_dev(mxb, cuda)
+    bsap.autotune(bm, bx, offsets=doff, reps=1)
+    got = bsap.broadphase_batched(bm, bx, doff).cpu().numpy().astype(np.uint32)
+    for s in range(24):
+        a, b = int(off[s]), int(off[s + 1])
+        sub = got[(got[:, 0] >= a) & (got[:, 0] < b)] - a
+        assert np.array_equal(sub, oracle_lib.bf_aabb(mnb[a:b], mxb[a:b])), s
