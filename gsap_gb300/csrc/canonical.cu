@@ -8,17 +8,61 @@
 // once and already counts pairs per row (first id, or both ids for the
 // both-direction format), so canonicalisation is a counting sort:
 //   1. exclusive look-back scan of the row counts -> row offsets;
-//   2. scatter each pair into its row(s), slots taken by atomic decrement of
-//      the row count (which leaves the counts at zero for the next call);
-//   3. sort each row by its second id;
+//   2. scatter each pair into its row(s) of an internal buffer, slots taken
+//      by atomic decrement of the row count (which leaves the counts at zero
+//      for the next call);
+//   3. place every pair at its final index: row offset + its rank by second
+//      id within the row (one thread per pair counting the row's smaller
+//      ids; rows are ~5-11 pairs long, so this costs sum(len^2) compares
+//      and needs no per-row sort network); rows longer than kRankRow are
+//      sorted by one warp each;
 //   4. (both-direction format) compact the offsets of the non-empty rows
 //      into pairEntries with a second scan.
 #include "internal.cuh"
 
 namespace gsap {
 
-constexpr int kScanItems = 8;
+constexpr int kScanItems = 16;
 constexpr int kScanTile = kThreads * kScanItems;
+
+// Warp-wide look-back over single-word tile states: lane k reads the word of
+// tile t-1-k, so a round trip covers 32 predecessors; aggregates are summed
+// up to the nearest inclusive prefix.  Returns the exclusive prefix of tile
+// t in every lane.  Bounded: on timeout sets kErrTimeout and returns what it
+// has (positions then stay in range, only too small).
+__device__ __forceinline__ uint32_t warp_lookback1(uint64_t* status, uint32_t t, uint32_t tag, uint32_t spin_limit,
+                                                   uint32_t* err) {
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t excl = 0, spins = 0;
+    int64_t top = (int64_t)t - 1;  // newest tile of the window
+    while (top >= 0) {
+        const int64_t j = top - (int64_t)lane;
+        uint64_t w = 0;
+        bool ready = true, pre = true;  // tiles before 0 act as a zero prefix
+        if (j >= 0) {
+            w = ld_lb_u64(status + j);
+            ready = (uint32_t)(w >> 32) == tag && (w & (kFlagAgg | kFlagPrefix));
+            pre = ready && (w & kFlagPrefix);
+        }
+        const uint32_t pm = __ballot_sync(0xffffffffu, pre);
+        const uint32_t nr = __ballot_sync(0xffffffffu, !ready);
+        const uint32_t p = pm ? (uint32_t)(__ffs(pm) - 1) : 32u;
+        const uint32_t need = p >= 31 ? 0xffffffffu : ((2u << p) - 1u);
+        if (nr & need) {
+            if (++spins > spin_limit) {
+                if (lane == 0) atomicOr(err, kErrTimeout);
+                return __shfl_sync(0xffffffffu, excl, 0);
+            }
+            if (spins > 16) __nanosleep(32);
+            continue;
+        }
+        uint32_t v = (j >= 0 && lane <= p) ? (uint32_t)(w & kValMask) : 0u;
+        excl += __reduce_add_sync(0xffffffffu, v);
+        if (p < 32) break;
+        top -= 32;
+    }
+    return excl;
+}
 
 // mode 0: out[i] = exclusive prefix of in[i] (i < n), out[n] = total.
 // mode 1: flag_i = rowoff[i+1] > rowoff[i]; entries[rank_i] = rowoff[i] for
@@ -41,14 +85,22 @@ __global__ void __launch_bounds__(kThreads) k_scan(BpScratch S, const uint32_t* 
         const uint32_t b = t * kScanTile + tid * kScanItems;
         uint32_t v[kScanItems];
         uint32_t sum = 0;
+        if (MODE == 0 && b + kScanItems <= n) {  // 64-byte aligned run: vector loads
+            const uint4* src = reinterpret_cast<const uint4*>(in + b);
 #pragma unroll
-        for (int k = 0; k < kScanItems; ++k) {
-            uint32_t i = b + k;
-            uint32_t x = 0;
-            if (i < n) x = MODE == 0 ? in[i] : (in[i + 1] > in[i] ? 1u : 0u);
-            v[k] = x;
-            sum += x;
+            for (int q = 0; q < kScanItems / 4; ++q) {
+                const uint4 x4 = src[q];
+                v[4 * q] = x4.x; v[4 * q + 1] = x4.y; v[4 * q + 2] = x4.z; v[4 * q + 3] = x4.w;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < kScanItems; ++k) {
+                const uint32_t i = b + k;
+                v[k] = i < n ? (MODE == 0 ? in[i] : (in[i + 1] > in[i] ? 1u : 0u)) : 0u;
+            }
         }
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) sum += v[k];
         // CTA exclusive scan of the thread sums
         uint32_t x = sum;
 #pragma unroll
@@ -64,30 +116,45 @@ __global__ void __launch_bounds__(kThreads) k_scan(BpScratch S, const uint32_t* 
             if ((uint32_t)w < wid) pre += s_w[w];
             tot += s_w[w];
         }
-        if (tid == 0) {
+        if (wid == 0) {
             uint64_t* st = S.status + t;
-            st_lb_u64(st, lb_word(tag, t == 0 ? kFlagPrefix : kFlagAgg, tot));
+            if (lane == 0) st_lb_u64(st, lb_word(tag, t == 0 ? kFlagPrefix : kFlagAgg, tot));
             uint32_t ex = 0;
             if (t > 0) {
-                ex = lookback(S.status, t, 0, 1, tag, spin, &C->error);
-                st_lb_u64(st, lb_word(tag, kFlagPrefix, ex + tot));
+                ex = warp_lookback1(S.status, t, tag, spin, &C->error);
+                if (lane == 0) st_lb_u64(st, lb_word(tag, kFlagPrefix, ex + tot));
             }
-            s_excl = ex;
-            if (t == ntiles - 1) {
-                if (MODE == 0) out[n] = ex + tot;
-                else C->scan_total = ex + tot;
+            if (lane == 0) {
+                s_excl = ex;
+                if (t == ntiles - 1) {
+                    if (MODE == 0) out[n] = ex + tot;
+                    else C->scan_total = ex + tot;
+                }
             }
         }
         __syncthreads();
         uint32_t run = s_excl + pre + x - sum;
+        if (MODE == 0 && b + kScanItems <= n) {
+            uint4* dst = reinterpret_cast<uint4*>(out + b);
 #pragma unroll
-        for (int k = 0; k < kScanItems; ++k) {
-            uint32_t i = b + k;
-            if (i < n) {
-                if (MODE == 0) out[i] = run;
-                else if (v[k] && run < entry_cap) entries[run] = (int32_t)in[i];
+            for (int q = 0; q < kScanItems / 4; ++q) {
+                uint4 o4;
+                o4.x = run; run += v[4 * q];
+                o4.y = run; run += v[4 * q + 1];
+                o4.z = run; run += v[4 * q + 2];
+                o4.w = run; run += v[4 * q + 3];
+                dst[q] = o4;
             }
-            run += v[k];
+        } else {
+#pragma unroll
+            for (int k = 0; k < kScanItems; ++k) {
+                const uint32_t i = b + k;
+                if (i < n) {
+                    if (MODE == 0) out[i] = run;
+                    else if (v[k] && run < entry_cap) entries[run] = (int32_t)in[i];
+                }
+                run += v[k];
+            }
         }
         __syncthreads();
     }
@@ -134,60 +201,40 @@ __global__ void __launch_bounds__(kThreads) k_scatter(BpScratch S, const uint2* 
     }
 }
 
-// Bitonic sorting network over N registers (every index is a compile-time
-// constant after unrolling, so v[] stays in registers).
-template <int N>
-__device__ __forceinline__ void bitonic_regs(uint32_t (&v)[N]) {
-#pragma unroll
-    for (int k = 2; k <= N; k <<= 1)
-#pragma unroll
-        for (int j = k >> 1; j > 0; j >>= 1)
-#pragma unroll
-            for (int i = 0; i < N; ++i) {
-                const int l = i ^ j;
-                if (l > i) {
-                    const bool up = (i & k) == 0;
-                    uint32_t a = v[i], b = v[l];
-                    bool sw = up ? (a > b) : (a < b);
-                    v[i] = sw ? b : a;
-                    v[l] = sw ? a : b;
-                }
-            }
-}
+constexpr uint32_t kRankRow = 256;  // longer rows go to k_rowsort_long
+constexpr int kLongRow = 1024;       // per-warp shared-memory sort limit
 
-template <int N>
-__device__ __forceinline__ void sort_row(uint2* out, uint64_t b, uint32_t len) {
-    uint32_t v[N];
-#pragma unroll
-    for (int k = 0; k < N; ++k) v[k] = ((uint32_t)k < len) ? out[b + k].y : 0xFFFFFFFFu;
-    bitonic_regs<N>(v);
-#pragma unroll
-    for (int k = 0; k < N; ++k)
-        if ((uint32_t)k < len) out[b + k].y = v[k];
-}
-
-// Sort every row by its second id: one thread per row with a register
-// network for rows of up to 32 pairs (rows average ~5-11 pairs); longer
-// rows are queued for k_rowsort_long.
-__global__ void __launch_bounds__(kThreads) k_rowsort(BpScratch S, uint2* out, uint64_t out_cap, uint32_t n) {
-    for (uint32_t r = blockIdx.x * kThreads + threadIdx.x; r < n; r += gridDim.x * kThreads) {
-        uint64_t b = S.rowoff[r], e = S.rowoff[r + 1];
-        if (e > out_cap) e = out_cap;
-        if (e <= b + 1) continue;
-        uint32_t len = (uint32_t)(e - b);
-        if (len <= 8) sort_row<8>(out, b, len);
-        else if (len <= 16) sort_row<16>(out, b, len);
-        else if (len <= 32) sort_row<32>(out, b, len);
-        else S.longrows[atomicAdd(&S.ctrl->long_rows, 1u)] = r;
+// Final placement: the pair at grouped index s (row x = its first id) goes
+// to rowoff[x] + (number of pairs of row x with a smaller second id).
+// Second ids are unique within a row, so the ranks are a permutation.
+// The lanes of a warp mostly share a row, so the row reads broadcast.
+__global__ void __launch_bounds__(kThreads) k_rank(BpScratch S, const uint2* __restrict__ grp, uint64_t grp_cap,
+                                                   uint32_t n, uint2* out, uint64_t out_cap) {
+    const uint64_t P = min((uint64_t)S.rowoff[n], grp_cap);  // grouped entries (2 per pair in both-direction form)
+    const uint64_t stride = (uint64_t)gridDim.x * kThreads;
+    for (uint64_t s = (uint64_t)blockIdx.x * kThreads + threadIdx.x; s < P; s += stride) {
+        const uint2 p = grp[s];
+        const uint32_t b = S.rowoff[p.x], e = S.rowoff[p.x + 1];
+        const uint32_t len = e - b;
+        if (len > kRankRow) {
+            if (s == b) S.longrows[atomicAdd(&S.ctrl->long_rows, 1u)] = p.x;  // queued once per row
+            continue;
+        }
+        uint32_t r = 0, k = b;
+        for (; k + 4 <= e; k += 4) {
+            const uint32_t y0 = grp[k].y, y1 = grp[k + 1].y, y2 = grp[k + 2].y, y3 = grp[k + 3].y;
+            r += (y0 < p.y) + (y1 < p.y) + (y2 < p.y) + (y3 < p.y);
+        }
+        for (; k < e; ++k) r += grp[k].y < p.y;
+        if ((uint64_t)b + r < out_cap) out[b + r] = p;
     }
 }
 
-constexpr int kLongRow = 1024;  // per-warp shared-memory sort limit
-
-// One warp per long row (rows of 33..1024 pairs; ~1% of rows at the 1M
-// workload): bitonic sort in the warp's slice of shared memory.  Longer rows
-// (pathological overlap) use an in-place odd-even transposition by the warp.
-__global__ void __launch_bounds__(kThreads) k_rowsort_long(BpScratch S, uint2* out, uint64_t out_cap) {
+// One warp per long row (more than kRankRow pairs; rare): bitonic sort of
+// the second ids in the warp's slice of shared memory for rows up to
+// kLongRow, rank placement by the warp beyond (pathological overlap).
+__global__ void __launch_bounds__(kThreads) k_rowsort_long(BpScratch S, const uint2* __restrict__ grp, uint2* out,
+                                                           uint64_t out_cap) {
     __shared__ uint32_t s_all[kThreads / 32][kLongRow];
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     uint32_t* s = s_all[wid];
@@ -195,14 +242,12 @@ __global__ void __launch_bounds__(kThreads) k_rowsort_long(BpScratch S, uint2* o
     const uint32_t warps = gridDim.x * (kThreads / 32);
     for (uint32_t q = blockIdx.x * (kThreads / 32) + wid; q < nlong; q += warps) {
         const uint32_t r = S.longrows[q];
-        uint64_t b = S.rowoff[r], e = S.rowoff[r + 1];
-        if (e > out_cap) e = out_cap;
-        if (e <= b + 1) continue;
-        const uint32_t len = (uint32_t)(e - b);
+        const uint32_t b = S.rowoff[r], e = S.rowoff[r + 1];
+        const uint32_t len = e - b;
         if (len <= (uint32_t)kLongRow) {
             uint32_t P = 32;
             while (P < len) P <<= 1;
-            for (uint32_t k = lane; k < P; k += 32) s[k] = k < len ? out[b + k].y : 0xFFFFFFFFu;
+            for (uint32_t k = lane; k < P; k += 32) s[k] = k < len ? grp[b + k].y : 0xFFFFFFFFu;
             __syncwarp();
             for (uint32_t k = 2; k <= P; k <<= 1)
                 for (uint32_t j = k >> 1; j > 0; j >>= 1) {
@@ -216,15 +261,15 @@ __global__ void __launch_bounds__(kThreads) k_rowsort_long(BpScratch S, uint2* o
                     }
                     __syncwarp();
                 }
-            for (uint32_t k = lane; k < len; k += 32) out[b + k].y = s[k];
+            for (uint32_t k = lane; k < len; k += 32)
+                if ((uint64_t)b + k < out_cap) out[b + k] = make_uint2(r, s[k]);
             __syncwarp();
         } else {
-            for (uint32_t phase = 0; phase < len; ++phase) {
-                for (uint32_t i = 2 * lane + (phase & 1); i + 1 < len; i += 64) {
-                    const uint32_t a = out[b + i].y, c = out[b + i + 1].y;
-                    if (a > c) { out[b + i].y = c; out[b + i + 1].y = a; }
-                }
-                __syncwarp();
+            for (uint32_t k = lane; k < len; k += 32) {
+                const uint32_t y = grp[b + k].y;
+                uint32_t rk = 0;
+                for (uint32_t m = b; m < e; ++m) rk += grp[m].y < y;
+                if ((uint64_t)b + rk < out_cap) out[b + rk] = make_uint2(r, y);
             }
         }
     }
@@ -235,9 +280,10 @@ cudaError_t launch_canonical(const BpScratch& s, uint32_t n, const uint2* in_pai
                              uint32_t spin, cudaStream_t st) {
     const int grid = sm_count() * 4;
     k_scan<0><<<grid, kThreads, 0, st>>>(s, s.rowcnt, s.rowoff, nullptr, 0, n, 5, spin);
-    k_scatter<<<sm_count() * 32, kThreads, 0, st>>>(s, in_pairs, in_cap, out_pairs, out_cap, both);
-    k_rowsort<<<(n + kThreads - 1) / kThreads, kThreads, 0, st>>>(s, out_pairs, out_cap, n);
-    k_rowsort_long<<<sm_count() * 2, kThreads, 0, st>>>(s, out_pairs, out_cap);
+    const uint64_t grp_cap = 2 * s.pair_cap_internal;
+    k_scatter<<<sm_count() * 32, kThreads, 0, st>>>(s, in_pairs, in_cap, s.grp_pairs, grp_cap, both);
+    k_rank<<<sm_count() * 16, kThreads, 0, st>>>(s, s.grp_pairs, grp_cap, n, out_pairs, out_cap);
+    k_rowsort_long<<<sm_count() * 2, kThreads, 0, st>>>(s, s.grp_pairs, out_pairs, out_cap);
     if (both && entries) k_scan<1><<<grid, kThreads, 0, st>>>(s, s.rowoff, nullptr, entries, entry_cap, n, 6, spin);
     return cudaGetLastError();
 }

@@ -97,10 +97,11 @@ struct BpScratch {
     // the object's lowest on u2, bit 1 when its row is the lowest on u3.
     float4* smin;
     float4* smax;
-    uint32_t* longrows;        // canonical output: ids of rows longer than 32
+    uint32_t* longrows;        // canonical output: ids of rows placed by k_rowsort_long
     uint32_t* rowcnt;          // per object pair counts (canonical output)
     uint32_t* rowoff;          // exclusive offsets, n+1
     uint32_t* tmp_pairs;       // unsorted pairs before canonicalisation
+    uint2* grp_pairs;          // pairs grouped by row, before the in-row order (canonical output)
     uint64_t entry_cap;
     uint64_t pair_cap_internal;
     uint64_t status_words;
