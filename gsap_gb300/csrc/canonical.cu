@@ -207,26 +207,36 @@ constexpr int kLongRow = 1024;       // per-warp shared-memory sort limit
 // Final placement: the pair at grouped index s (row x = its first id) goes
 // to rowoff[x] + (number of pairs of row x with a smaller second id).
 // Second ids are unique within a row, so the ranks are a permutation.
-// The lanes of a warp mostly share a row, so the row reads broadcast.
+// A CTA owns the rows that start in its tile [lo, hi) of the grouped list;
+// a row of at most kRankRow pairs then lies inside [lo, hi + kRankRow), which
+// the CTA stages in shared memory with coalesced loads, so the rank loops
+// run on shared memory instead of chaining L2 round trips.
+constexpr uint32_t kRankTile = 2048;
 __global__ void __launch_bounds__(kThreads) k_rank(BpScratch S, const uint2* __restrict__ grp, uint64_t grp_cap,
                                                    uint32_t n, uint2* out, uint64_t out_cap) {
-    const uint64_t P = min((uint64_t)S.rowoff[n], grp_cap);  // grouped entries (2 per pair in both-direction form)
-    const uint64_t stride = (uint64_t)gridDim.x * kThreads;
-    for (uint64_t s = (uint64_t)blockIdx.x * kThreads + threadIdx.x; s < P; s += stride) {
-        const uint2 p = grp[s];
-        const uint32_t b = S.rowoff[p.x], e = S.rowoff[p.x + 1];
-        const uint32_t len = e - b;
-        if (len > kRankRow) {
-            if (s == b) S.longrows[atomicAdd(&S.ctrl->long_rows, 1u)] = p.x;  // queued once per row
-            continue;
+    __shared__ uint2 s_p[kRankTile + kRankRow];
+    const uint32_t P = (uint32_t)min((uint64_t)S.rowoff[n], grp_cap);  // grouped entries
+    const uint32_t ntiles = (P + kRankTile - 1) / kRankTile;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint32_t lo = tile * kRankTile;
+        const uint32_t hi = min(lo + kRankTile, P);
+        const uint32_t wend = min(hi + kRankRow, P);
+        for (uint32_t s = lo + threadIdx.x; s < wend; s += kThreads) s_p[s - lo] = grp[s];
+        __syncthreads();
+        for (uint32_t s = lo + threadIdx.x; s < wend; s += kThreads) {
+            const uint2 p = s_p[s - lo];
+            const uint32_t b = __ldg(S.rowoff + p.x);
+            if (b < lo || b >= hi) continue;  // row owned by another tile
+            const uint32_t e = __ldg(S.rowoff + p.x + 1), len = e - b;
+            if (len > kRankRow) {
+                if (s == b) S.longrows[atomicAdd(&S.ctrl->long_rows, 1u)] = p.x;  // queued once per row
+                continue;
+            }
+            uint32_t r = 0;
+            for (uint32_t k = b - lo; k < e - lo; ++k) r += s_p[k].y < p.y;
+            if ((uint64_t)b + r < out_cap) out[b + r] = p;
         }
-        uint32_t r = 0, k = b;
-        for (; k + 4 <= e; k += 4) {
-            const uint32_t y0 = grp[k].y, y1 = grp[k + 1].y, y2 = grp[k + 2].y, y3 = grp[k + 3].y;
-            r += (y0 < p.y) + (y1 < p.y) + (y2 < p.y) + (y3 < p.y);
-        }
-        for (; k < e; ++k) r += grp[k].y < p.y;
-        if ((uint64_t)b + r < out_cap) out[b + r] = p;
+        __syncthreads();
     }
 }
 
@@ -282,7 +292,7 @@ cudaError_t launch_canonical(const BpScratch& s, uint32_t n, const uint2* in_pai
     k_scan<0><<<grid, kThreads, 0, st>>>(s, s.rowcnt, s.rowoff, nullptr, 0, n, 5, spin);
     const uint64_t grp_cap = 2 * s.pair_cap_internal;
     k_scatter<<<sm_count() * 32, kThreads, 0, st>>>(s, in_pairs, in_cap, s.grp_pairs, grp_cap, both);
-    k_rank<<<sm_count() * 16, kThreads, 0, st>>>(s, s.grp_pairs, grp_cap, n, out_pairs, out_cap);
+    k_rank<<<sm_count() * 8, kThreads, 0, st>>>(s, s.grp_pairs, grp_cap, n, out_pairs, out_cap);
     k_rowsort_long<<<sm_count() * 2, kThreads, 0, st>>>(s, s.grp_pairs, out_pairs, out_cap);
     if (both && entries) k_scan<1><<<grid, kThreads, 0, st>>>(s, s.rowoff, nullptr, entries, entry_cap, n, 6, spin);
     return cudaGetLastError();
