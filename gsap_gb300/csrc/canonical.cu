@@ -8,9 +8,10 @@
 // once and already counts pairs per row (first id, or both ids for the
 // both-direction format), so canonicalisation is a counting sort:
 //   1. exclusive look-back scan of the row counts -> row offsets;
-//   2. scatter each pair into its row(s) of an internal buffer, slots taken
-//      by atomic decrement of the row count (which leaves the counts at zero
-//      for the next call);
+//   2. scatter each pair into its row(s) of an internal buffer at the slot
+//      the sweep drew from the row counter when it stored the pair (the
+//      scan has read the counters and put them back to zero for the next
+//      call);
 //   3. place every pair at its final index: row offset + its rank by second
 //      id within the row (one thread per pair counting the row's smaller
 //      ids; rows are ~5-11 pairs long, so this costs sum(len^2) compares
@@ -67,10 +68,10 @@ __device__ __forceinline__ uint32_t warp_lookback1(uint64_t* status, uint32_t t,
 // mode 0: out[i] = exclusive prefix of in[i] (i < n), out[n] = total.
 // mode 1: flag_i = rowoff[i+1] > rowoff[i]; entries[rank_i] = rowoff[i] for
 //         flagged rows; total -> ctrl->scan_total.
+// mode 0 also zeroes in[0..n) once read (the row counters of the next call).
 template <int MODE>
-__global__ void __launch_bounds__(kThreads) k_scan(BpScratch S, const uint32_t* __restrict__ in, uint32_t* out,
-                                                   int32_t* entries, uint64_t entry_cap, uint32_t n, int slot,
-                                                   uint32_t spin) {
+__global__ void __launch_bounds__(kThreads) k_scan(BpScratch S, uint32_t* in, uint32_t* out, int32_t* entries,
+                                                   uint64_t entry_cap, uint32_t n, int slot, uint32_t spin) {
     __shared__ uint32_t s_w[8];
     __shared__ uint32_t s_tile, s_excl;
     const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -86,17 +87,19 @@ __global__ void __launch_bounds__(kThreads) k_scan(BpScratch S, const uint32_t* 
         uint32_t v[kScanItems];
         uint32_t sum = 0;
         if (MODE == 0 && b + kScanItems <= n) {  // 64-byte aligned run: vector loads
-            const uint4* src = reinterpret_cast<const uint4*>(in + b);
+            uint4* src = reinterpret_cast<uint4*>(in + b);
 #pragma unroll
             for (int q = 0; q < kScanItems / 4; ++q) {
                 const uint4 x4 = src[q];
                 v[4 * q] = x4.x; v[4 * q + 1] = x4.y; v[4 * q + 2] = x4.z; v[4 * q + 3] = x4.w;
+                src[q] = make_uint4(0u, 0u, 0u, 0u);
             }
         } else {
 #pragma unroll
             for (int k = 0; k < kScanItems; ++k) {
                 const uint32_t i = b + k;
                 v[k] = i < n ? (MODE == 0 ? in[i] : (in[i + 1] > in[i] ? 1u : 0u)) : 0u;
+                if (MODE == 0 && i < n) in[i] = 0u;
             }
         }
 #pragma unroll
@@ -160,43 +163,23 @@ __global__ void __launch_bounds__(kThreads) k_scan(BpScratch S, const uint32_t* 
     }
 }
 
-// Scatter pairs into their rows.  both: row i gets (i, j) and row j (j, i).
-// Each thread takes 4 pairs and issues their returning atomics back to back,
-// so the grid keeps many of them in flight instead of chaining one per
-// thread.
-constexpr int kScatterPer = 4;
+// Scatter pairs into their rows at the slots the sweep drew.  both: row i
+// gets (i, j) and row j (j, i).  No atomics.
 __global__ void __launch_bounds__(kThreads) k_scatter(BpScratch S, const uint2* __restrict__ in, uint64_t in_cap,
                                                       uint2* out, uint64_t out_cap, int both) {
     const uint64_t P = min((uint64_t)S.ctrl->pair_count, in_cap);
     const uint32_t* off = S.rowoff;
+    const uint2* __restrict__ rank = S.tmp_rank;
     const uint64_t stride = (uint64_t)gridDim.x * kThreads;
-    for (uint64_t k0 = (uint64_t)blockIdx.x * kThreads + threadIdx.x; k0 < P; k0 += stride * kScatterPer) {
-        uint2 p[kScatterPer];
-        uint32_t a[kScatterPer], b[kScatterPer];
-#pragma unroll
-        for (int u = 0; u < kScatterPer; ++u) {
-            uint64_t k = k0 + u * stride;
-            p[u] = k < P ? in[k] : make_uint2(0xFFFFFFFFu, 0xFFFFFFFFu);
-        }
-#pragma unroll
-        for (int u = 0; u < kScatterPer; ++u)
-            if (p[u].x != 0xFFFFFFFFu) a[u] = atomicSub(&S.rowcnt[p[u].x], 1u);
+    for (uint64_t k = (uint64_t)blockIdx.x * kThreads + threadIdx.x; k < P; k += stride) {
+        const uint2 p = in[k], r = rank[k];
+        const uint64_t s = (uint64_t)__ldg(off + p.x) + r.x;
+        if (s < out_cap) out[s] = p;
+        else atomicOr(&S.ctrl->error, kErrPairCap);
         if (both) {
-#pragma unroll
-            for (int u = 0; u < kScatterPer; ++u)
-                if (p[u].x != 0xFFFFFFFFu) b[u] = atomicSub(&S.rowcnt[p[u].y], 1u);
-        }
-#pragma unroll
-        for (int u = 0; u < kScatterPer; ++u) {
-            if (p[u].x == 0xFFFFFFFFu) continue;
-            uint64_t s = (uint64_t)off[p[u].x] + a[u] - 1u;
-            if (s < out_cap) out[s] = p[u];
+            const uint64_t s2 = (uint64_t)__ldg(off + p.y) + r.y;
+            if (s2 < out_cap) out[s2] = make_uint2(p.y, p.x);
             else atomicOr(&S.ctrl->error, kErrPairCap);
-            if (both) {
-                uint64_t s2 = (uint64_t)off[p[u].y] + b[u] - 1u;
-                if (s2 < out_cap) out[s2] = make_uint2(p[u].y, p[u].x);
-                else atomicOr(&S.ctrl->error, kErrPairCap);
-            }
         }
     }
 }
@@ -291,7 +274,7 @@ cudaError_t launch_canonical(const BpScratch& s, uint32_t n, const uint2* in_pai
     const int grid = sm_count() * 4;
     k_scan<0><<<grid, kThreads, 0, st>>>(s, s.rowcnt, s.rowoff, nullptr, 0, n, 5, spin);
     const uint64_t grp_cap = 2 * s.pair_cap_internal;
-    k_scatter<<<sm_count() * 32, kThreads, 0, st>>>(s, in_pairs, in_cap, s.grp_pairs, grp_cap, both);
+    k_scatter<<<sm_count() * 16, kThreads, 0, st>>>(s, in_pairs, in_cap, s.grp_pairs, grp_cap, both);
     k_rank<<<sm_count() * 8, kThreads, 0, st>>>(s, s.grp_pairs, grp_cap, n, out_pairs, out_cap);
     k_rowsort_long<<<sm_count() * 2, kThreads, 0, st>>>(s, s.grp_pairs, out_pairs, out_cap);
     if (both && entries) k_scan<1><<<grid, kThreads, 0, st>>>(s, s.rowoff, nullptr, entries, entry_cap, n, 6, spin);

@@ -73,20 +73,37 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
     uint64_t tests = 0;
     uint32_t steps = 0;
 
+    // Reserves global space for the warp's buffered pairs and stores them.
+    // For the canonical output each stored pair also takes its slot in its
+    // row (and, both-direction form, in its second id's row) from the row
+    // counters; the returning atomics of a lane's pairs are issued together.
     auto flush = [&]() {
         __syncwarp();
         unsigned long long base = 0;
         if (lane == 0 && nbuf) base = atomicAdd(&C->pair_count, (unsigned long long)nbuf);
         base = __shfl_sync(0xffffffffu, base, 0);
-        for (uint32_t k = lane; k < nbuf; k += 32) {
-            uint2 p = s_buf[wid][k];
-            if (base + k < pair_cap) {  // rows count stored pairs only: the scatter undoes exactly these
-                pairs[base + k] = p;
+        constexpr int kPer = kBuf / 32;
+        uint2 p[kPer], rk[kPer];
+        bool st[kPer];
+#pragma unroll
+        for (int u = 0; u < kPer; ++u) {
+            const uint32_t k = lane + 32u * u;
+            st[u] = k < nbuf && base + k < pair_cap;  // rows count stored pairs only
+            rk[u] = make_uint2(0u, 0u);
+            if (st[u]) {
+                p[u] = s_buf[wid][k];
                 if (count_rows) {
-                    atomicAdd(&S.rowcnt[p.x], 1u);
-                    if (count_rows == 2) atomicAdd(&S.rowcnt[p.y], 1u);
+                    rk[u].x = atomicAdd(&S.rowcnt[p[u].x], 1u);
+                    if (count_rows == 2) rk[u].y = atomicAdd(&S.rowcnt[p[u].y], 1u);
                 }
             }
+        }
+#pragma unroll
+        for (int u = 0; u < kPer; ++u) {
+            if (!st[u]) continue;
+            const uint64_t k = base + lane + 32u * u;
+            pairs[k] = p[u];
+            if (count_rows) S.tmp_rank[k] = rk[u];
         }
         __syncwarp();
         nbuf = 0;
