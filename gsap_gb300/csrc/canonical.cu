@@ -171,15 +171,32 @@ __global__ void __launch_bounds__(kThreads) k_scatter(BpScratch S, const uint2* 
     const uint32_t* off = S.rowoff;
     const uint2* __restrict__ rank = S.tmp_rank;
     const uint64_t stride = (uint64_t)gridDim.x * kThreads;
-    for (uint64_t k = (uint64_t)blockIdx.x * kThreads + threadIdx.x; k < P; k += stride) {
-        const uint2 p = in[k], r = rank[k];
-        const uint64_t s = (uint64_t)__ldg(off + p.x) + r.x;
-        if (s < out_cap) out[s] = p;
-        else atomicOr(&S.ctrl->error, kErrPairCap);
-        if (both) {
-            const uint64_t s2 = (uint64_t)__ldg(off + p.y) + r.y;
-            if (s2 < out_cap) out[s2] = make_uint2(p.y, p.x);
+    constexpr int kPer = 4;  // pairs per thread with their row-offset loads in flight together
+    for (uint64_t k0 = (uint64_t)blockIdx.x * kThreads + threadIdx.x; k0 < P; k0 += stride * kPer) {
+        uint2 p[kPer], r[kPer];
+        uint32_t o1[kPer], o2[kPer];
+#pragma unroll
+        for (int u = 0; u < kPer; ++u) {
+            const uint64_t k = k0 + u * stride;
+            if (k < P) { p[u] = in[k]; r[u] = rank[k]; }
+        }
+#pragma unroll
+        for (int u = 0; u < kPer; ++u) {
+            if (k0 + u * stride >= P) continue;
+            o1[u] = __ldg(off + p[u].x);
+            if (both) o2[u] = __ldg(off + p[u].y);
+        }
+#pragma unroll
+        for (int u = 0; u < kPer; ++u) {
+            if (k0 + u * stride >= P) continue;
+            const uint64_t s = (uint64_t)o1[u] + r[u].x;
+            if (s < out_cap) out[s] = p[u];
             else atomicOr(&S.ctrl->error, kErrPairCap);
+            if (both) {
+                const uint64_t s2 = (uint64_t)o2[u] + r[u].y;
+                if (s2 < out_cap) out[s2] = make_uint2(p[u].y, p[u].x);
+                else atomicOr(&S.ctrl->error, kErrPairCap);
+            }
         }
     }
 }

@@ -52,8 +52,9 @@ __device__ __forceinline__ bool load_box(const BpArgs& A, uint32_t i, float3& a,
     return isfinite(a.x) && isfinite(a.y) && isfinite(a.z) && isfinite(b.x) && isfinite(b.y) && isfinite(b.z);
 }
 
-constexpr int kProjItems = 8;                          // objects per thread per half
-constexpr int kProjHalf = kThreads * kProjItems;       // a chunk is processed in two halves
+constexpr int kProjItems = 8;                          // objects per thread
+constexpr int kProjHalf = kThreads * kProjItems;       // objects per CTA: half a work chunk
+constexpr int kProjSplit = kChunk / kProjHalf;         // CTAs per work chunk
 
 template <int PASSES>
 __global__ void __launch_bounds__(kThreads) k_project(BpScratch S, BpArgs A) {
@@ -64,7 +65,7 @@ __global__ void __launch_bounds__(kThreads) k_project(BpScratch S, BpArgs A) {
     __shared__ uint32_t s_base;
     const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     uint32_t scene, b, e, wfirst, nw;
-    if (!map_work(blockIdx.x, S, A, scene, b, e, wfirst, nw)) return;
+    if (!map_work(blockIdx.x / kProjSplit, S, A, scene, b, e, wfirst, nw)) return;
     for (uint32_t k = tid; k < PASSES * 256; k += kThreads) (&s_hist[0][0])[k] = 0u;
     if (tid == 0) {
         const Scene& sc = S.scenes[scene];
@@ -86,7 +87,8 @@ __global__ void __launch_bounds__(kThreads) k_project(BpScratch S, BpArgs A) {
     const float qmax = (float)((1u << Q) - 1u);
 
     bool bad = false;
-    for (int half = 0; half < kChunk / kProjHalf; ++half) {
+    {
+    const uint32_t half = blockIdx.x % kProjSplit;
     uint32_t qlo[kProjItems], clo[kProjItems], ncl[kProjItems], pre[kProjItems];
     uint32_t running = 0;
     const uint32_t wb = b + half * kProjHalf + wid * (32 * kProjItems);
@@ -153,7 +155,6 @@ __global__ void __launch_bounds__(kThreads) k_project(BpScratch S, BpArgs A) {
                 }
             }
     }
-    __syncthreads();  // s_wtot / s_base are reused by the next half
     }
     if (bad) atomicOr(&S.ctrl->error, kErrNonFinite);
     __syncthreads();
@@ -164,8 +165,8 @@ __global__ void __launch_bounds__(kThreads) k_project(BpScratch S, BpArgs A) {
 }
 
 cudaError_t launch_project(const BpScratch& s, const BpArgs& a, int passes, cudaStream_t st) {
-    if (passes == 3) k_project<3><<<a.num_work, kThreads, 0, st>>>(s, a);
-    else k_project<4><<<a.num_work, kThreads, 0, st>>>(s, a);
+    if (passes == 3) k_project<3><<<a.num_work * kProjSplit, kThreads, 0, st>>>(s, a);
+    else k_project<4><<<a.num_work * kProjSplit, kThreads, 0, st>>>(s, a);
     return cudaGetLastError();
 }
 
