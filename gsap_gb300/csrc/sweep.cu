@@ -46,6 +46,7 @@ __device__ __forceinline__ float proj_hi(const float* u, float3 a, float3 b) {
 }
 
 constexpr int kBuf = 128;  // pairs buffered per warp before a global reservation
+constexpr uint32_t kGrab = 4;  // 32-entry chunks taken per work-counter atomic
 constexpr int kWarps = kThreads / 32;
 
 template <int MODE>
@@ -109,12 +110,19 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
         nbuf = 0;
     };
 
+    // Work is taken kGrab chunks of 32 entries at a time: every atomic on the
+    // one shared counter serialises at its L2 slice, so fewer, larger grabs.
+    uint32_t base = 0, grab_end = 0;
     while (true) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(&C->sweep_ctr, 32u);
-        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= grab_end) {
+            uint32_t g = 0;
+            if (lane == 0) g = atomicAdd(&C->sweep_ctr, 32u * kGrab);
+            base = __shfl_sync(0xffffffffu, g, 0);
+            grab_end = base + 32u * kGrab;
+        }
         if (base >= E) break;
         const uint32_t e = base + lane;
+        base += 32u;
         uint32_t run = 0;  // candidates of entry e: e+1 .. e+run
         float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), pb = pa;
         uint32_t i = 0;
