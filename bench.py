@@ -433,20 +433,38 @@ def run_extras(args, dev, stream):
                       "frac": round(bbytes / (batched_ms / 1e3) / 1e9 / peak, 4)}
     del bsap, pairs, dmn, dmx
     torch.cuda.empty_cache()
-    # --- rigid body: 65,536 cubes of 2x2x2 particles in a 200^3 box
+    # --- rigid body: 65,536 cubes of 2x2x2 particles in a 200^3 box, 1000 steps
     nb = args.bodies
     sc = scenes.cubes_in_box(nb, box=200.0, seed=3)
+    cfgp = dict(k=2e4, eta=50.0, kt=0.1, gravity_y=-9.81, box_lo=(0.0, 0.0, 0.0), box_hi=(200.0, 200.0, 200.0))
     prb = ParticleRigidBody(nb, sc["n_particles"], 16)
     prb.load_scene(sc)
-    prb.set_contact(model=CONTACT_CONFIG, k=2e4, eta=50.0, kt=0.1, gravity_y=-9.81, box_lo=(0, 0, 0),
-                    box_hi=(200, 200, 200))
+    prb.set_contact(model=CONTACT_CONFIG, **cfgp)
     rsap = Sap(nb)
     dt = 1.0 / 600.0
+    # one step from the initial state against the FP64 oracle (CPU)
+    err = None
+    if not args.no_cpu:
+        import oracle
+        oracle.build()
+        st64 = scenes.to_f64(sc)
+        t0 = time.perf_counter()
+        oracle.rb_step_cfg_f64(st64, dict(cfgp, dt=dt))
+        cpu_rb_s = time.perf_counter() - t0
+        prb.step(rsap, dt, stream=stream)
+        torch.cuda.synchronize()
+        g = prb.get_state()
+
+        def rel(a, b):
+            return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-30))
+        err = {"pos": rel(g["pos"][:, :3], st64["pos"][:, :3]), "vel": rel(g["lin_vel"][:, :3], st64["lin_vel"][:, :3])}
+        prb.load_scene(sc)
     for _ in range(5):
         prb.step(rsap, dt, stream=stream)
     torch.cuda.synchronize()
     rsap.check()
-    steps = 100
+    Pb_rb = int(rsap.stats()["pairs"])
+    steps = 1000
     e0.record(stream)
     for _ in range(steps):
         prb.step(rsap, dt, stream=stream)
@@ -454,9 +472,71 @@ def run_extras(args, dev, stream):
     torch.cuda.synchronize()
     rsap.check()
     rb_ms = e0.elapsed_time(e1) / steps
-    Pb_rb = int(L.gsap_sap_check(rsap.handle, None) == 0)  # handle still healthy
-    out["rigid"] = {"bodies": nb, "particles": sc["n_particles"], "ms_per_step": round(rb_ms, 4),
-                    "body_steps_per_s": round(nb / (rb_ms / 1e3), 1), "healthy": bool(Pb_rb)}
+    npart = sc["n_particles"]
+    b_rb = rb_algorithmic_bytes(nb, npart, 64 * Pb_rb, Pb_rb)
+    rb = {"bodies": nb, "particles": npart, "steps": steps, "ms_per_step": round(rb_ms, 4),
+          "body_steps_per_s": round(nb / (rb_ms / 1e3), 1), "body_pairs": Pb_rb,
+          "bytes_alg": b_rb, "achieved_gbs": round(b_rb / (rb_ms / 1e3) / 1e9, 1),
+          "frac": round(b_rb / (rb_ms / 1e3) / 1e9 / peak, 4),
+          "formula": "276 n_b + 96 n_p + 8 P_c + B_bp(n_b, P_b), P_c = 64 P_b particle pairs tested"}
+    if err is not None:
+        rb["step1_rel_err_vs_fp64"] = err
+        rb["cpu_baseline"] = {"value": round(nb / cpu_rb_s / 1e6, 4), "unit": "Mbody_steps/s", "cores": os.cpu_count(),
+                              "kind": "port", "sample": "one config-model step of the same scene, FP64 oracle "
+                                                        "(oracle/rb.c orc_rb_step_cfg_f64, OpenMP)"}
+    out["rigid"] = rb
+    del prb, rsap
+    torch.cuda.empty_cache()
+
+    # --- batched dynamics: 1024 scenes of 256..8192 bodies (cubes, rods, L shapes) in a 100^3 box
+    ms_ = scenes.mixed_scenes(S=args.rb_scenes, seed=4)
+    bo = ms_["body_offsets"]
+    nbb = int(bo[-1])
+    cfgb = dict(cfgp, box_hi=(100.0, 100.0, 100.0))
+    bprb = ParticleRigidBody(nbb, ms_["n_particles"], 16)
+    bprb.load_scene(ms_)
+    bprb.set_contact(model=CONTACT_CONFIG, **cfgb)
+    bprb.set_scenes(bo)
+    bsap2 = Sap(nbb, max_scenes=args.rb_scenes)
+    for _ in range(3):
+        bprb.step(bsap2, dt, stream=stream)
+    torch.cuda.synchronize()
+    bsap2.check()
+    bsteps = 100
+    e0.record(stream)
+    for _ in range(bsteps):
+        bprb.step(bsap2, dt, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    bsap2.check()
+    b_ms = e0.elapsed_time(e1) / bsteps
+    # plain: the first 32 scenes, one system per scene, stepped one after another
+    nplain = 32
+    plain = []
+    for s in range(nplain):
+        a, z = int(bo[s]), int(bo[s + 1])
+        sub = scenes.subset_bodies(ms_, a, z)
+        p = ParticleRigidBody(z - a, sub["n_particles"], 16)
+        p.load_scene(sub)
+        p.set_contact(model=CONTACT_CONFIG, **cfgb)
+        plain.append((p, Sap(z - a)))
+    for p, sp in plain:
+        p.step(sp, dt, stream=stream)
+    torch.cuda.synchronize()
+    psteps = 20
+    e0.record(stream)
+    for _ in range(psteps):
+        for p, sp in plain:
+            p.step(sp, dt, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    p_ms = e0.elapsed_time(e1) / psteps
+    out["rigid_batched"] = {"scenes": args.rb_scenes, "bodies": nbb, "particles": ms_["n_particles"],
+                            "ms_per_step": round(b_ms, 4),
+                            "scene_steps_per_s": round(args.rb_scenes / (b_ms / 1e3), 1),
+                            "plain_scene_steps_per_s": round(nplain / (p_ms / 1e3), 1),
+                            "plain_sample": f"first {nplain} scenes, one system each, stepped in turn",
+                            "speedup_vs_plain": round((args.rb_scenes / b_ms) / (nplain / p_ms), 2)}
     return out
 
 
@@ -514,6 +594,7 @@ def main():
     ap.add_argument("--n", type=int, default=N_OBJ)
     ap.add_argument("--scenes", type=int, default=4096)
     ap.add_argument("--bodies", type=int, default=65536)
+    ap.add_argument("--rb-scenes", type=int, default=1024)
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cell-factor", type=float, default=None,

@@ -186,6 +186,20 @@ def mixed_scenes(S: int = 1024, seed: int = 0, lo: int = 256, hi: int = 8192, bo
     return out
 
 
+def subset_bodies(sc: dict, a: int, z: int) -> dict:
+    """Bodies [a, z) of a scene dict as a scene of their own (particle
+    starts re-based; shape tables shared)."""
+    out = {k: np.ascontiguousarray(sc[k][a:z]) for k in ("pos", "quat", "lin_vel", "ang_vel", "shape_idx",
+                                                          "n_part", "inv_mass", "inv_inertia")}
+    ps = np.zeros(z - a, np.int32)
+    ps[1:] = np.cumsum(out["n_part"])[:-1]
+    out["p_start"] = ps
+    for k in ("ref_pos", "ref_mass", "shape_inv_inertia", "shape_inv_inertia64"):
+        out[k] = sc[k]
+    out["n_particles"] = int(out["n_part"].sum())
+    return out
+
+
 def to_f64(sc: dict) -> dict:
     """State dict for the FP64 oracle (oracle.rb_step_cfg_f64)."""
     nb, np_ = len(sc["pos"]), sc["n_particles"]
