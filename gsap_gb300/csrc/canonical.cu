@@ -169,7 +169,8 @@ __global__ void __launch_bounds__(kThreads) k_scatter(BpScratch S, const uint2* 
                                                       uint2* out, uint64_t out_cap, int both) {
     const uint64_t P = min((uint64_t)S.ctrl->pair_count, in_cap);
     const uint32_t* off = S.rowoff;
-    const uint2* __restrict__ rank = S.tmp_rank;
+    const uint32_t* __restrict__ rank1 = S.tmp_rank;
+    const uint2* __restrict__ rank2 = reinterpret_cast<const uint2*>(S.tmp_rank);
     const uint64_t stride = (uint64_t)gridDim.x * kThreads;
     constexpr int kPer = 4;  // pairs per thread with their row-offset loads in flight together
     for (uint64_t k0 = (uint64_t)blockIdx.x * kThreads + threadIdx.x; k0 < P; k0 += stride * kPer) {
@@ -178,7 +179,10 @@ __global__ void __launch_bounds__(kThreads) k_scatter(BpScratch S, const uint2* 
 #pragma unroll
         for (int u = 0; u < kPer; ++u) {
             const uint64_t k = k0 + u * stride;
-            if (k < P) { p[u] = in[k]; r[u] = rank[k]; }
+            if (k < P) {
+                p[u] = in[k];
+                r[u] = both ? rank2[k] : make_uint2(rank1[k], 0u);
+            }
         }
 #pragma unroll
         for (int u = 0; u < kPer; ++u) {

@@ -102,7 +102,8 @@ struct BpScratch {
     uint32_t* rowoff;          // exclusive offsets, n+1
     uint32_t* tmp_pairs;       // unsorted pairs before canonicalisation
     uint2* grp_pairs;          // pairs grouped by row, before the in-row order (canonical output)
-    uint2* tmp_rank;           // per unsorted pair: its slot in row first (x) and row second (y)
+    uint32_t* tmp_rank;        // per unsorted pair k: its slot in row first (rank[k]); both-direction
+                               // form: slots in row first and row second (rank[2k], rank[2k + 1])
     uint64_t entry_cap;
     uint64_t pair_cap_internal;
     uint64_t status_words;

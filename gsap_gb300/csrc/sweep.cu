@@ -104,7 +104,8 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
             if (!st[u]) continue;
             const uint64_t k = base + lane + 32u * u;
             pairs[k] = p[u];
-            if (count_rows) S.tmp_rank[k] = rk[u];
+            if (count_rows == 2) reinterpret_cast<uint2*>(S.tmp_rank)[k] = rk[u];
+            else if (count_rows) S.tmp_rank[k] = rk[u].x;
         }
         __syncwarp();
         nbuf = 0;
