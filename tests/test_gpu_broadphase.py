@@ -186,3 +186,43 @@ def test_autotune_keeps_the_pair_set(cuda, oracle_lib):
         a, b = int(off[s]), int(off[s + 1])
         sub = got[(got[:, 0] >= a) & (got[:, 0] < b)] - a
         assert np.array_equal(sub, oracle_lib.bf_aabb(mnb[a:b], mxb[a:b])), s
+
+
+@pytest.mark.parametrize("sort_bits", [24, 32])
+@pytest.mark.parametrize("cell_factor", [0.5, 1.0, 2.0, 4.0])
+def test_every_setting_gives_the_same_pairs(cuda, oracle_lib, sort_bits, cell_factor):
+    """Key width and cell size only move work between stages: the pair set
+    is the brute force's for every setting the autotuner may pick."""
+    from gsap_gb300 import Sap, scenes
+    n = 30_000
+    c, h, _ = scenes.aabb_gauss_parts(n, seed=21, std=(25.0, 6.0, 2.0))
+    mn = np.concatenate([c - h, np.zeros((n, 1), np.float32)], 1)
+    mx = np.concatenate([c + h, np.zeros((n, 1), np.float32)], 1)
+    sap = Sap(n, sort_bits=sort_bits, cell_factor=cell_factor)
+    assert np.array_equal(run_bp(sap, mn, mx, cuda), oracle_lib.bf_aabb(mn, mx))
+    assert np.array_equal(run_bp(sap, mn, mx, cuda, sorted=False), oracle_lib.bf_aabb(mn, mx))
+
+
+def test_batched_with_empty_and_tiny_scenes(cuda, oracle_lib):
+    """Scenes of 0, 1 and 2 objects between ordinary ones: no pair crosses a
+    scene edge and the small scenes produce what brute force says."""
+    import torch
+    from gsap_gb300 import Sap, scenes
+    sizes = [0, 1, 500, 0, 2, 1, 3000, 0, 64, 1, 2, 700]
+    rng = np.random.default_rng(9)
+    mns, mxs = [], []
+    for m in sizes:
+        cc = rng.uniform(0, 20, (m, 3)).astype(np.float32)
+        hh = rng.uniform(0.1, 1.5, (m, 3)).astype(np.float32)
+        mns.append(np.concatenate([cc - hh, np.zeros((m, 1), np.float32)], 1))
+        mxs.append(np.concatenate([cc + hh, np.zeros((m, 1), np.float32)], 1))
+    mn, mx = np.concatenate(mns), np.concatenate(mxs)
+    off = np.zeros(len(sizes) + 1, np.int64)
+    off[1:] = np.cumsum(sizes)
+    bsap = Sap(len(mn), max_scenes=len(sizes))
+    got = bsap.broadphase_batched(to_dev(mn, cuda), to_dev(mx, cuda),
+                                  torch.from_numpy(off.astype(np.int32)).to(cuda)).cpu().numpy().astype(np.uint32)
+    want = [oracle_lib.bf_aabb(mn[a:b], mx[a:b]).astype(np.int64) + a
+            for a, b in zip(off[:-1], off[1:]) if b - a >= 2]
+    want = np.concatenate(want).astype(np.uint32)
+    assert np.array_equal(got, want)
