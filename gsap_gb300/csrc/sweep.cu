@@ -55,11 +55,11 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
                                                     uint64_t pair_cap, int count_rows) {
     __shared__ uint2 s_buf[kWarps][kBuf];
     // entries of the warp's chunk that have candidates, in run order
-    __shared__ float4 s_pa[kWarps][32];
-    __shared__ float4 s_pb[kWarps][MODE == 0 ? 32 : 1];
+    // (boxes: (lo.xyz, jb), (hi.xyz, flags); spheres: (centre, radius),
+    // (jb, flags, -, -)); the candidate of test t is jb + t
+    __shared__ float4 s_t0[kWarps][32];
+    __shared__ float4 s_t1[kWarps][32];
     __shared__ uint32_t s_id[kWarps][32];  // object index
-    __shared__ uint32_t s_jb[kWarps][32];  // candidate of test t is s_jb + t
-    __shared__ uint32_t s_fl[kWarps][32];  // owner flags
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const uint32_t lt = lanemask_lt();
     const uint32_t le = lt | (1u << lane);
@@ -177,11 +177,15 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
         const uint32_t nz = __ballot_sync(0xffffffffu, run > 0);
         if (run > 0) {
             const uint32_t r = __popc(nz & lt);
-            s_pa[wid][r] = pa;
-            if (MODE == 0) s_pb[wid][r] = pb;
+            const uint32_t jb = e + 1u - start;
+            if (MODE == 0) {
+                s_t0[wid][r] = make_float4(pa.x, pa.y, pa.z, __uint_as_float(jb));
+                s_t1[wid][r] = make_float4(pb.x, pb.y, pb.z, __uint_as_float(fl));
+            } else {
+                s_t0[wid][r] = pa;
+                s_t1[wid][r] = make_float4(__uint_as_float(jb), __uint_as_float(fl), 0.f, 0.f);
+            }
             s_id[wid][r] = i;
-            s_jb[wid][r] = e + 1u - start;
-            s_fl[wid][r] = fl;
         }
         __syncwarp();
         tests += total;
@@ -195,13 +199,13 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
             uint32_t o = 0, oi = 0;
             if (t < total) {
                 const uint32_t m = before + __popc(starts & le) - 1u;  // run of test t
-                const uint32_t j = s_jb[wid][m] + t;
-                const float4 ea = s_pa[wid][m];
+                const float4 ea = s_t0[wid][m], eb = s_t1[wid][m];
+                const uint32_t j = __float_as_uint(MODE == 0 ? ea.w : eb.x) + t;
+                const uint32_t efl = __float_as_uint(MODE == 0 ? eb.w : eb.y);
                 const float4 qa = __ldg(smin + j);
                 bool ov;
                 uint32_t jid, jfl;
                 if (MODE == 0) {
-                    const float4 eb = s_pb[wid][m];
                     const float4 qb = __ldg(smax + j);
                     jid = __float_as_uint(qa.w);
                     jfl = __float_as_uint(qb.w);
@@ -216,7 +220,7 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
                     float rr = __fadd_rn(ea.w, qa.w);
                     ov = t1 < __fmul_rn(rr, rr);
                 }
-                if (ov && (s_fl[wid][m] | jfl) == 3u) {
+                if (ov && (efl | jfl) == 3u) {
                     hit = true;
                     o = jid;
                     oi = s_id[wid][m];
