@@ -257,15 +257,17 @@ static gsap_status record(gsap_sap* h, const Call& c, cudaStream_t st, bool time
     SortGather gather{c.mn, c.mode == GSAP_MODE_AABB ? c.mx : nullptr, s.objcell, s.objscene, s.scenes,
                       s.smin, s.smax};
     for (int p = 0; p < passes; ++p) {
-        CK(launch_sort_pass(s, p, passes, s.keys[src], s.vals[src], s.keys[src ^ 1], s.vals[src ^ 1], count,
-                            s.entry_cap, a.spin_limit, st, p == passes - 1 ? &gather : nullptr, true));
+        // the last pass's object ids go into the sweep records, not into a value array
+        const bool last = p == passes - 1;
+        CK(launch_sort_pass(s, p, passes, s.keys[src], s.vals[src], s.keys[src ^ 1], last ? nullptr : s.vals[src ^ 1],
+                            count, s.entry_cap, a.spin_limit, st, last ? &gather : nullptr, true));
         src ^= 1;
     }
     mark();
     const bool canon = (c.flags & GSAP_FLAG_SORTED) || c.both;
     uint2* sweep_out = canon ? (uint2*)s.tmp_pairs : c.pairs;
     uint64_t sweep_cap = canon ? s.pair_cap_internal : c.cap;
-    CK(launch_sweep(s, a, s.keys[src], s.vals[src], sweep_out, sweep_cap, canon ? (c.both ? 2 : 1) : 0, st));
+    CK(launch_sweep(s, a, s.keys[src], sweep_out, sweep_cap, canon ? (c.both ? 2 : 1) : 0, st));
     mark();
     if (canon) {
         CK(launch_canonical(s, c.n, (const uint2*)s.tmp_pairs, s.pair_cap_internal, c.pairs, c.cap, c.both,

@@ -148,7 +148,7 @@ cudaError_t launch_sort_pass(const BpScratch& s, int pass, int passes, const uin
                              const SortGather* gather = nullptr, bool count_next = false);
 cudaError_t launch_sort_prep(const BpScratch& s, const uint32_t* keys, const uint32_t* count_ptr,
                              uint32_t n, int passes, cudaStream_t st);
-cudaError_t launch_sweep(const BpScratch& s, const BpArgs& a, const uint32_t* keys, const uint32_t* vals,
+cudaError_t launch_sweep(const BpScratch& s, const BpArgs& a, const uint32_t* keys,
                          uint2* pairs, uint64_t pair_cap, int count_rows, cudaStream_t st);
 cudaError_t launch_canonical(const BpScratch& s, uint32_t n, const uint2* in_pairs, uint64_t in_cap,
                              uint2* out_pairs, uint64_t out_cap, int both, int32_t* entries,

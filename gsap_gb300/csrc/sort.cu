@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_onesweep(BpScratch S, const uin
                 continue;
             }
             kout[g] = kk;
-            vout[g] = vv;
+            if (vout) vout[g] = vv;
             if (G.smin) {  // last pass of the broadphase: entries in sorted order
                 // owner flags: is this entry's cell the object's lowest
                 // column (u2) / row (u3)?  A pair is owned by the cell of

@@ -51,7 +51,7 @@ constexpr int kWarps = kThreads / 32;
 
 template <int MODE>
 __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const uint32_t* __restrict__ keys,
-                                                    const uint32_t* __restrict__ vals, uint2* __restrict__ pairs,
+                                                    uint2* __restrict__ pairs,
                                                     uint64_t pair_cap, int count_rows) {
     __shared__ uint2 s_buf[kWarps][kBuf];
     // entries of the warp's chunk that have candidates, in run order
@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
     }
 }
 
-cudaError_t launch_sweep(const BpScratch& s, const BpArgs& a, const uint32_t* keys, const uint32_t* vals,
+cudaError_t launch_sweep(const BpScratch& s, const BpArgs& a, const uint32_t* keys,
                          uint2* pairs, uint64_t pair_cap, int count_rows, cudaStream_t st) {
     static int grid[2] = {0, 0};
     int m = a.mode == 1 ? 1 : 0;
@@ -255,8 +255,8 @@ cudaError_t launch_sweep(const BpScratch& s, const BpArgs& a, const uint32_t* ke
         else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep<1>, kThreads, 0);
         grid[m] = sm_count() * (per_sm > 0 ? per_sm : 1);
     }
-    if (m == 0) k_sweep<0><<<grid[m], kThreads, 0, st>>>(s, a, keys, vals, pairs, pair_cap, count_rows);
-    else k_sweep<1><<<grid[m], kThreads, 0, st>>>(s, a, keys, vals, pairs, pair_cap, count_rows);
+    if (m == 0) k_sweep<0><<<grid[m], kThreads, 0, st>>>(s, a, keys, pairs, pair_cap, count_rows);
+    else k_sweep<1><<<grid[m], kThreads, 0, st>>>(s, a, keys, pairs, pair_cap, count_rows);
     return cudaGetLastError();
 }
 
