@@ -95,6 +95,7 @@ SIGNATURES = [
     ("gsap_k_update_velocity", I32, [P, P, P, P, P, P, P, P, P, P, I32, F32, F32, I32, I32, P]),
     ("gsap_debug_scene_solve", C.c_int, [C.POINTER(F64), C.POINTER(F64), C.POINTER(F64), F64, U32, U32, F32,
                                          U32, U64, C.POINTER(F64)]),
+    ("gsap_debug_lookback_timeout", C.c_int, [P, U32, P]),
     ("gsap_debug_stats", C.c_int, [P, C.POINTER(U64), P]),
     ("gsap_debug_sizes", C.c_int, [C.POINTER(U32)]),
 ]

@@ -606,6 +606,22 @@ extern "C" int gsap_debug_stats(gsap_sap* h, uint64_t* out8, void* stream) {
     return 0;
 }
 
+// One thread waits on look-back words that nothing publishes (slot 7 is
+// used by no pass), with the pipeline's bounded wait.
+__global__ void k_debug_lookback(BpScratch S, uint32_t spin_limit) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const uint32_t tag = (S.ctrl->epoch << 3) | 7u;
+    (void)lookback(S.status, 1, 0, 1, tag, spin_limit, &S.ctrl->error);
+}
+
+extern "C" int gsap_debug_lookback_timeout(gsap_sap* h, uint32_t spin_limit, void* stream) {
+    if (!h) return fail(GSAP_ERR_INVALID, "null handle");
+    cudaStream_t st = (cudaStream_t)stream;
+    k_debug_lookback<<<1, 32, 0, st>>>(h->s, spin_limit);
+    CK(cudaGetLastError());
+    return finish(h, st, nullptr, ~0ull);
+}
+
 extern "C" int gsap_debug_sizes(uint32_t* out) {
     if (!out) return -1;
     out[0] = sizeof(Ctrl);

@@ -26,6 +26,14 @@ int gsap_debug_scene_solve(const double* sums18, const double* hmax3, const doub
 struct gsap_sap;
 int gsap_debug_stats(struct gsap_sap* h, uint64_t* out8, void* stream);
 
+/* Failure-path check of the bounded device waits (needs a GPU): one thread
+ * runs the radix look-back on a tile whose predecessor never publishes (a
+ * tag no pass uses), so the wait gives up after spin_limit polls, sets the
+ * timeout bit of the handle's error word and returns.  The call then reads
+ * and clears the error word like any broadphase call: it returns
+ * GSAP_ERR_DEVICE_TIMEOUT and leaves the handle and the context usable. */
+int gsap_debug_lookback_timeout(struct gsap_sap* h, uint32_t spin_limit, void* stream);
+
 /* Sizes of internal device structures (control block, scene record, PCA
  * partial, sort tile) for layout checks.  Returns 0. */
 int gsap_debug_sizes(uint32_t* out4);

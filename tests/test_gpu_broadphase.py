@@ -226,3 +226,19 @@ def test_batched_with_empty_and_tiny_scenes(cuda, oracle_lib):
             for a, b in zip(off[:-1], off[1:]) if b - a >= 2]
     want = np.concatenate(want).astype(np.uint32)
     assert np.array_equal(got, want)
+
+
+def test_bounded_wait_reports_timeout_and_recovers(cuda, oracle_lib):
+    """A device wait on a predecessor that never publishes gives up after its
+    poll limit and reports GSAP_ERR_DEVICE_TIMEOUT; nothing hangs, and the
+    same handle then produces the exact pair set."""
+    import torch
+    from gsap_gb300 import Sap, _lib, scenes
+    sap = Sap(4096)
+    L = _lib.load()
+    st = L.gsap_debug_lookback_timeout(sap.handle, 1000, None)
+    assert st == 4  # GSAP_ERR_DEVICE_TIMEOUT
+    assert b"iteration cap" in L.gsap_last_error()
+    torch.cuda.synchronize()
+    mn, mx = scenes.aabb_uniform(4096, 3)
+    assert np.array_equal(run_bp(sap, mn, mx, cuda), oracle_lib.bf_aabb(mn, mx))
