@@ -234,6 +234,24 @@ def run_ours(args, world, rank, local):
     traffic = traffic_table().get((f"stage_{dom}", "gauss1m"))
     pipe_gbs = alg["total"] / (ms / 1e3) / 1e9
 
+    # temporal mode (GSAP_FLAG_TEMPORAL): each call sweeps with the previous
+    # call's grid while its own PCA runs beside it; same inputs, same pairs
+    for k in range(min(len(dsets), args.steps) + 2):
+        sap.broadphase_async(*dsets[k % len(dsets)], pairs, d_count, sorted=True, graph=True, temporal=True,
+                             stream=stream)
+    torch.cuda.synchronize()
+    sap.check()
+    assert int(d_count.item()) > 0
+    et0, et1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    et0.record(stream)
+    for k in range(args.steps):
+        sap.broadphase_async(*dsets[k % len(dsets)], pairs, d_count, sorted=True, graph=True, temporal=True,
+                             stream=stream)
+    et1.record(stream)
+    torch.cuda.synchronize()
+    sap.check()
+    temporal_ms = et0.elapsed_time(et1) / args.steps
+
     # unsorted pair set (no canonicalisation), for reference
     for k in range(16):
         call(k, sorted_=False)
@@ -352,6 +370,9 @@ def run_ours(args, world, rank, local):
                         "qbits": stats["qbits"], "warp_iters": stats["iters"],
                         "lane_efficiency": round(stats["tests"] / max(1, 32 * stats["iters"]), 3)},
         "unsorted_ms_per_step": round(unsorted_ms, 4),
+        "temporal": {"ms_per_step": round(temporal_ms, 4), "value": round(n / (temporal_ms / 1e3) / 1e6, 3),
+                     "unit": "Mobjects/s",
+                     "mode": "GSAP_FLAG_TEMPORAL: grid of the previous call, this call's PCA beside the sweep"},
         "e2e": {"value": round(e2e_val, 3), "unit": "Mobjects/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": int(np.mean(d2h)), "calls": K_e2e,
                 "mode": "pinned H2D of inputs + D2H of count and pairs every call; copies of one call overlap "

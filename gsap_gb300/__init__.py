@@ -6,11 +6,11 @@ this package is the host-side mirror of the reference's ``Sap`` and
 ``ParticleRigidBody`` classes.  PyTorch is used only for device memory and
 streams.
 """
-from ._lib import (AXIS_PCA, AXIS_REF, CONTACT_CONFIG, CONTACT_REF, FLAG_GRAPH, FLAG_SORTED, MODE_AABB,
-                   MODE_SPHERE, GsapError, load)
+from ._lib import (AXIS_PCA, AXIS_REF, CONTACT_CONFIG, CONTACT_REF, FLAG_GRAPH, FLAG_SORTED, FLAG_TEMPORAL,
+                   MODE_AABB, MODE_SPHERE, GsapError, load)
 
 __all__ = ["Sap", "ParticleRigidBody", "GsapError", "load", "MODE_AABB", "MODE_SPHERE", "AXIS_PCA",
-           "AXIS_REF", "FLAG_SORTED", "FLAG_GRAPH", "CONTACT_REF", "CONTACT_CONFIG"]
+           "AXIS_REF", "FLAG_SORTED", "FLAG_GRAPH", "FLAG_TEMPORAL", "CONTACT_REF", "CONTACT_CONFIG"]
 
 
 def __getattr__(name):

@@ -17,7 +17,7 @@ STATUS_NAMES = {0: "GSAP_OK", 1: "GSAP_ERR_INVALID", 2: "GSAP_ERR_CAPACITY", 3: 
                 4: "GSAP_ERR_DEVICE_TIMEOUT", 5: "GSAP_ERR_NONFINITE"}
 MODE_AABB, MODE_SPHERE = 0, 1
 AXIS_PCA, AXIS_REF = 0, 1
-FLAG_SORTED, FLAG_GRAPH = 0x1, 0x2
+FLAG_SORTED, FLAG_GRAPH, FLAG_TEMPORAL = 0x1, 0x2, 0x4
 CONTACT_REF, CONTACT_CONFIG = 0, 1
 
 

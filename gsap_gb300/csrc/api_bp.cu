@@ -107,11 +107,18 @@ struct gsap_sap {
     cudaEvent_t ev[8];
     float stage_ms[6];
     int nstages;
+    // temporal mode: a side stream for the PCA branch, and what the
+    // parameters in the scratch were last computed for
+    cudaStream_t side;
+    cudaEvent_t ev_fork, ev_join;
+    bool tp_valid;
+    uint32_t tp_n, tp_S, tp_mode, tp_bits, tp_axis;
+    float tp_cf;
 };
 
 static void free_scratch(gsap_sap* h) {
     BpScratch& s = h->s;
-    void* ptrs[] = {s.ctrl, s.scenes, s.partials, s.scene_done, s.work_start, s.objcell, s.objscene,
+    void* ptrs[] = {s.ctrl, s.scenes, s.scenes_next, s.partials, s.scene_done, s.work_start, s.objcell, s.objscene,
                     s.keys[0], s.keys[1], s.vals[0], s.vals[1], s.status, s.rowcnt, s.rowoff, s.tmp_pairs,
                     s.grp_pairs, s.tmp_rank, s.smin, s.smax, s.longrows};
     for (void* p : ptrs)
@@ -123,6 +130,9 @@ static void free_scratch(gsap_sap* h) {
         h->graphs = nullptr;
     }
     if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
+    if (h->side) cudaStreamDestroy(h->side);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
     for (auto& e : h->ev)
         if (e) cudaEventDestroy(e);
 }
@@ -162,6 +172,7 @@ extern "C" gsap_sap* gsap_sap_create(uint32_t max_n, const gsap_config* cfg) {
     };
     A((void**)&s.ctrl, sizeof(Ctrl));
     A((void**)&s.scenes, sizeof(Scene) * c.max_scenes);
+    A((void**)&s.scenes_next, sizeof(Scene) * c.max_scenes);
     A((void**)&s.partials, sizeof(PcaPartial) * s.max_work);
     A((void**)&s.scene_done, 4ull * c.max_scenes);
     A((void**)&s.work_start, 4ull * (c.max_scenes + 1));
@@ -184,6 +195,9 @@ extern "C" gsap_sap* gsap_sap_create(uint32_t max_n, const gsap_config* cfg) {
     if (ok && cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking) != cudaSuccess) ok = false;
     for (auto& e : h->ev)
         if (ok && cudaEventCreate(&e) != cudaSuccess) ok = false;
+    if (ok && cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess) ok = false;
+    if (ok && cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess) ok = false;
+    if (ok && cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess) ok = false;
     if (!ok) {
         cudaError_t e = cudaGetLastError();
         fail(GSAP_ERR_CUDA, "gsap_sap_create: allocation failed (%s)", cudaGetErrorString(e));
@@ -227,6 +241,26 @@ struct Call {
     int both;           // 1: Sap::collision format
 };
 
+// Temporal mode is used when asked for and the scratch holds parameters
+// computed for a call of the same shape; otherwise the call runs the plain
+// pipeline (its TEMPORAL bit cleared, so it also has its own cached graph).
+static void temporal_resolve(gsap_sap* h, Call& c) {
+    if (!(c.flags & GSAP_FLAG_TEMPORAL)) return;
+    const bool ok = h->tp_valid && !h->timing && h->tp_n == c.n && h->tp_S == c.S && h->tp_mode == (uint32_t)c.mode &&
+                    h->tp_bits == h->cfg.sort_bits && h->tp_axis == h->cfg.axis_mode && h->tp_cf == h->cfg.cell_factor;
+    if (!ok) c.flags &= ~GSAP_FLAG_TEMPORAL;
+}
+
+static void temporal_note(gsap_sap* h, const Call& c) {
+    h->tp_valid = true;
+    h->tp_n = c.n;
+    h->tp_S = c.S;
+    h->tp_mode = (uint32_t)c.mode;
+    h->tp_bits = h->cfg.sort_bits;
+    h->tp_axis = h->cfg.axis_mode;
+    h->tp_cf = h->cfg.cell_factor;
+}
+
 static gsap_status record(gsap_sap* h, const Call& c, cudaStream_t st, bool timed) {
     BpScratch& s = h->s;
     BpArgs a;
@@ -247,8 +281,21 @@ static gsap_status record(gsap_sap* h, const Call& c, cudaStream_t st, bool time
         if (timed) cudaEventRecord(h->ev[ev++], st);
     };
     mark();
+    const bool temporal = (c.flags & GSAP_FLAG_TEMPORAL) != 0;
     if (c.off) CK(launch_plan(s, a, st));
-    CK(launch_pca(s, a, st));
+    if (temporal) {
+        // The projection, sort and sweep of this call use the parameters of
+        // the previous call (already in the scratch); this call's PCA runs
+        // beside them and prepares the next call's.  Any grid gives the same
+        // pair set, so the result is exact either way.
+        CK(cudaEventRecord(h->ev_fork, st));
+        CK(cudaStreamWaitEvent(h->side, h->ev_fork, 0));
+        CK(launch_pca(s, a, h->side, 1));
+        CK(cudaEventRecord(h->ev_join, h->side));
+        CK(launch_reset(s, st));
+    } else {
+        CK(launch_pca(s, a, st));
+    }
     mark();
     CK(launch_project(s, a, passes, st));
     mark();
@@ -273,6 +320,10 @@ static gsap_status record(gsap_sap* h, const Call& c, cudaStream_t st, bool time
         CK(launch_canonical(s, c.n, (const uint2*)s.tmp_pairs, s.pair_cap_internal, c.pairs, c.cap, c.both,
                             c.entries, c.ecap, a.spin_limit, st));
         mark();
+    }
+    if (temporal) {
+        CK(cudaStreamWaitEvent(st, h->ev_join, 0));
+        CK(launch_commit(s, c.S, st));
     }
     if (c.d_count) CK(cudaMemcpyAsync(c.d_count, &s.ctrl->pair_count, 8, cudaMemcpyDeviceToDevice, st));
     if (timed) h->nstages = ev - 1;
@@ -333,6 +384,7 @@ static gsap_status finish(gsap_sap* h, cudaStream_t st, uint64_t* count_out, uin
     memcpy(&cnt, (char*)h->h_ctrl + 16, 8);
     if (count_out) *count_out = cnt;
     if (err) {
+        h->tp_valid = false;  // the next call recomputes its parameters first
         CK(cudaMemsetAsync(&h->s.ctrl->error, 0, 4, st));
         CK(cudaStreamSynchronize(st));
         if (err & kErrTimeout) return fail(GSAP_ERR_DEVICE_TIMEOUT, "a device-side wait exceeded its iteration cap");
@@ -386,8 +438,10 @@ static gsap_status broadphase(gsap_sap* h, const float* d_min, const float* d_ma
     c.cap = cap;
     c.d_count = d_count;
     c.flags = flags;
+    temporal_resolve(h, c);
     gsap_status r = run(h, c, st);
     if (r != GSAP_OK) return r;
+    temporal_note(h, c);
     // sorted output goes through the internal pair buffer first
     uint64_t eff = (flags & GSAP_FLAG_SORTED) ? (cap < h->s.pair_cap_internal ? cap : h->s.pair_cap_internal) : cap;
     if (h_count) return finish(h, st, h_count, eff);
@@ -498,6 +552,7 @@ extern "C" gsap_status gsap_sap_collision(gsap_sap* h, float spacing, const floa
     c.both = 1;
     gsap_status r = run(h, c, st);
     if (r != GSAP_OK) return r;
+    temporal_note(h, c);
     uint64_t np = 0;
     uint64_t half = pair_cap / 2;
     r = finish(h, st, &np, half < h->s.pair_cap_internal ? half : h->s.pair_cap_internal);
@@ -661,5 +716,7 @@ gsap_status gsap::bp_both_async(gsap_sap* h, int mode, const float4* mn, const f
         CK(cudaMemsetAsync(h->s.rowoff, 0, 4ull * (n + 1), st));
         return GSAP_OK;
     }
-    return record(h, c, st, false);
+    gsap_status r = record(h, c, st, false);
+    if (r == GSAP_OK) temporal_note(h, c);
+    return r;
 }

@@ -49,6 +49,9 @@ struct Ctrl {
     unsigned long long tests; // sweep: candidate pairs tested (diagnostics)
     unsigned long long iters; // sweep: warp iterations of the candidate loop (diagnostics)
     uint32_t hist[kMaxPasses][256];
+    // temporal mode: the key layout computed from this call's input for the
+    // next call (committed at the end of the call)
+    uint32_t qbits_next, key_bits_next, total_buckets_next, pad_next;
 };
 
 // Per-scene parameters written by the PCA kernel.
@@ -84,6 +87,7 @@ struct BpScratch {
     Scene* scenes;
     PcaPartial* partials;
     uint32_t* scene_done;      // per-scene PCA completion counters
+    Scene* scenes_next;        // temporal mode: per-scene parameters for the next call
     uint32_t* work_start;      // per-scene first work item (S+1), batched plan
     uint32_t* objcell;         // per object: (c2lo << 16) | c3lo
     uint32_t* objscene;        // per object scene id (batched only)
@@ -129,7 +133,13 @@ struct BpArgs {
 // ---------------------------------------------------------------- launches
 // Each returns cudaGetLastError() of its launch.
 cudaError_t launch_plan(const BpScratch& s, const BpArgs& a, cudaStream_t st);
-cudaError_t launch_pca(const BpScratch& s, const BpArgs& a, cudaStream_t st);
+// temporal != 0: the finish writes the parameters into scenes_next and the
+// *_next layout fields and leaves the pipeline counters alone (the main
+// branch resets them with launch_reset and adopts the new parameters with
+// launch_commit once both branches have finished).
+cudaError_t launch_pca(const BpScratch& s, const BpArgs& a, cudaStream_t st, int temporal = 0);
+cudaError_t launch_reset(const BpScratch& s, cudaStream_t st);
+cudaError_t launch_commit(const BpScratch& s, uint32_t num_scenes, cudaStream_t st);
 cudaError_t launch_project(const BpScratch& s, const BpArgs& a, int passes, cudaStream_t st);
 // Gather epilogue of the last sort pass: entry g also gets the bounds of its
 // object and its owner flags, so the sweep reads candidates in order.

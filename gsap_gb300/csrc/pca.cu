@@ -160,7 +160,8 @@ __global__ void __launch_bounds__(kThreads) k_pca(BpScratch S, BpArgs A) {
 // scene to finish computes the global bucket bases and the key layout and
 // resets the counters of the later stages.  A separate launch keeps the FP64
 // tail's registers out of the streaming kernel.
-__global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, uint64_t entry_cap) {
+__global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, uint64_t entry_cap, int temporal) {
+    Scene* const out = temporal ? S.scenes_next : S.scenes;
     __shared__ uint32_t s_flag;
     const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const uint32_t scene = blockIdx.x;
@@ -222,7 +223,7 @@ __global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, 
         z.n = (double)(se - sb);
         Scene sc;
         choose_scene(z, A, entry_cap, A.n, sc);
-        S.scenes[scene] = sc;
+        out[scene] = sc;
         __threadfence();
         uint32_t old = atomicAdd(&C->scenes_done, 1u);
         s_flag = (old == A.num_scenes - 1) ? 1u : 0u;
@@ -238,7 +239,7 @@ __global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, 
     for (uint32_t base = 0; base < A.num_scenes; base += kThreads) {
         uint32_t s = base + tid;
         uint32_t v = 0;
-        if (s < A.num_scenes) v = __ldcg(&S.scenes[s].G2) * __ldcg(&S.scenes[s].G3);
+        if (s < A.num_scenes) v = __ldcg(&out[s].G2) * __ldcg(&out[s].G3);
         uint32_t x = v;
         for (int o = 1; o < 32; o <<= 1) {
             uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
@@ -249,7 +250,7 @@ __global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, 
         uint32_t pre = 0;
         for (uint32_t w = 0; w < wid; ++w) pre += s_wsum[w];
         uint32_t excl = s_carry + pre + x - v;
-        if (s < A.num_scenes) S.scenes[s].bucket_base = excl;
+        if (s < A.num_scenes) out[s].bucket_base = excl;
         __syncthreads();
         if (tid == kThreads - 1) s_carry = excl + v;
         __syncthreads();
@@ -263,9 +264,23 @@ __global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, 
         if (q > 24) q = 24;
         if (q == 0) atomicOr(&C->error, kErrCellRange);
         s_q = q;
-        C->qbits = q;
+        C->scenes_done = 0;
+        if (temporal) {
+            C->qbits_next = q;
+            C->key_bits_next = A.key_bits;
+            C->total_buckets_next = total;
+        }
+    }
+    if (temporal) {  // the main branch owns the pipeline counters
+        __syncthreads();
+        const float qf = (float)(1u << s_q);
+        for (uint32_t s = tid; s < A.num_scenes; s += kThreads) out[s].q_scale = __fdiv_rn(qf, __ldcg(&out[s].q_range));
+        return;
+    }
+    if (tid == 0) {
+        C->qbits = s_q;
         C->key_bits = A.key_bits;
-        C->total_buckets = total;
+        C->total_buckets = s_carry;
         C->entry_count = 0;
         C->pair_count = 0ull;
         for (int p = 0; p < kMaxPasses + 4; ++p) C->tile_ctr[p] = 0;
@@ -276,13 +291,12 @@ __global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, 
         C->tests = 0ull;
         C->iters = 0ull;
         C->epoch = C->epoch + 1u;
-        C->scenes_done = 0;
     }
     for (int p = 0; p < kMaxPasses; ++p) C->hist[p][tid] = 0u;
     __syncthreads();
     // quantisation scale of every scene, computed once for all kernels
     const float qf = (float)(1u << s_q);
-    for (uint32_t s = tid; s < A.num_scenes; s += kThreads) S.scenes[s].q_scale = __fdiv_rn(qf, __ldcg(&S.scenes[s].q_range));
+    for (uint32_t s = tid; s < A.num_scenes; s += kThreads) out[s].q_scale = __fdiv_rn(qf, __ldcg(&out[s].q_range));
 }
 
 cudaError_t launch_plan(const BpScratch& s, const BpArgs& a, cudaStream_t st) {
@@ -290,9 +304,51 @@ cudaError_t launch_plan(const BpScratch& s, const BpArgs& a, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_pca(const BpScratch& s, const BpArgs& a, cudaStream_t st) {
+cudaError_t launch_pca(const BpScratch& s, const BpArgs& a, cudaStream_t st, int temporal) {
     k_pca<<<a.num_work, kThreads, 0, st>>>(s, a);
-    k_pca_finish<<<a.num_scenes, kThreads, 0, st>>>(s, a, s.entry_cap);
+    k_pca_finish<<<a.num_scenes, kThreads, 0, st>>>(s, a, s.entry_cap, temporal);
+    return cudaGetLastError();
+}
+
+// Temporal mode, main branch: the counter resets that the finish does in the
+// plain pipeline.
+__global__ void k_reset(BpScratch S) {
+    Ctrl* C = S.ctrl;
+    const uint32_t tid = threadIdx.x;
+    if (tid == 0) {
+        C->entry_count = 0;
+        C->pair_count = 0ull;
+        for (int p = 0; p < kMaxPasses + 4; ++p) C->tile_ctr[p] = 0;
+        C->sweep_ctr = 0;
+        C->scan_ctr = 0;
+        C->scan_total = 0;
+        C->long_rows = 0;
+        C->tests = 0ull;
+        C->iters = 0ull;
+        C->epoch = C->epoch + 1u;
+    }
+    for (int p = 0; p < kMaxPasses; ++p) C->hist[p][tid] = 0u;
+}
+
+// Temporal mode, after both branches: the parameters computed from this
+// call's input become the ones the next call uses.
+__global__ void k_commit(BpScratch S, uint32_t num_scenes) {
+    for (uint32_t s = threadIdx.x; s < num_scenes; s += blockDim.x) S.scenes[s] = S.scenes_next[s];
+    if (threadIdx.x == 0) {
+        Ctrl* C = S.ctrl;
+        C->qbits = C->qbits_next;
+        C->key_bits = C->key_bits_next;
+        C->total_buckets = C->total_buckets_next;
+    }
+}
+
+cudaError_t launch_reset(const BpScratch& s, cudaStream_t st) {
+    k_reset<<<1, 256, 0, st>>>(s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_commit(const BpScratch& s, uint32_t num_scenes, cudaStream_t st) {
+    k_commit<<<1, 256, 0, st>>>(s, num_scenes);
     return cudaGetLastError();
 }
 

@@ -14,7 +14,7 @@ import ctypes as C
 import torch
 
 from . import _lib
-from ._lib import (AXIS_PCA, FLAG_GRAPH, FLAG_SORTED, MODE_AABB, MODE_SPHERE, Config, GsapError,
+from ._lib import (AXIS_PCA, FLAG_GRAPH, FLAG_SORTED, FLAG_TEMPORAL, MODE_AABB, MODE_SPHERE, Config, GsapError,
                    check, load)
 
 
@@ -113,7 +113,7 @@ class Sap:
 
     # ----------------------------------------------------------- AABB form
     def broadphase(self, mn: torch.Tensor, mx: torch.Tensor | None = None, pairs: torch.Tensor | None = None,
-                   sorted: bool = True, graph: bool = False, stream=None) -> torch.Tensor:
+                   sorted: bool = True, graph: bool = False, temporal: bool = False, stream=None) -> torch.Tensor:
         """Overlapping pairs (i < j) as an (P, 2) int32 tensor (uint32 ids).
 
         mn / mx: (n, 4) float32 CUDA tensors (AABB min / max; for the sphere
@@ -121,7 +121,7 @@ class Sap:
         n = mn.shape[0]
         _dev_ptr(mn, "mn", torch.float32, 4)
         _dev_ptr(mx, "mx", torch.float32, 4)
-        flags = (FLAG_SORTED if sorted else 0) | (FLAG_GRAPH if graph else 0)
+        flags = (FLAG_SORTED if sorted else 0) | (FLAG_GRAPH if graph else 0) | (FLAG_TEMPORAL if temporal else 0)
         if pairs is None:
             pairs = torch.empty((max(16, 8 * n), 2), dtype=torch.int32, device=mn.device)
         for _ in range(2):
@@ -159,11 +159,12 @@ class Sap:
                                        C.c_void_p(_stream_ptr(stream))))
         return {"sort_bits": int(cfg.sort_bits), "cell_factor": float(cfg.cell_factor)}
 
-    def broadphase_async(self, mn, mx, pairs, d_count, sorted=False, graph=False, stream=None):
+    def broadphase_async(self, mn, mx, pairs, d_count, sorted=False, graph=False, temporal=False, stream=None):
         """Asynchronous form: the pair count goes to the device tensor
         d_count (one int64); no host synchronisation.  Errors are picked up by
-        check()."""
-        flags = (FLAG_SORTED if sorted else 0) | (FLAG_GRAPH if graph else 0)
+        check().  temporal: sweep with the previous call's grid while this
+        call's PCA runs beside it (GSAP_FLAG_TEMPORAL)."""
+        flags = (FLAG_SORTED if sorted else 0) | (FLAG_GRAPH if graph else 0) | (FLAG_TEMPORAL if temporal else 0)
         st = load().gsap_broadphase_aabb(self._h, mn.data_ptr(), mx.data_ptr() if mx is not None else None,
                                          C.c_uint32(mn.shape[0]), pairs.data_ptr(), C.c_uint64(pairs.shape[0]),
                                          C.c_void_p(d_count.data_ptr()), None, C.c_uint32(flags),
@@ -172,13 +173,13 @@ class Sap:
 
     def broadphase_batched(self, mn: torch.Tensor, mx: torch.Tensor | None, offsets: torch.Tensor,
                            pairs: torch.Tensor | None = None, sorted: bool = True, graph: bool = False,
-                           stream=None) -> torch.Tensor:
+                           temporal: bool = False, stream=None) -> torch.Tensor:
         """Batched scenes: offsets is a CUDA int32 tensor of S+1 scene
         starts.  Pairs use global ids and never cross scenes."""
         n = mn.shape[0]
         S = offsets.numel() - 1
         _dev_ptr(offsets, "offsets", torch.int32)
-        flags = (FLAG_SORTED if sorted else 0) | (FLAG_GRAPH if graph else 0)
+        flags = (FLAG_SORTED if sorted else 0) | (FLAG_GRAPH if graph else 0) | (FLAG_TEMPORAL if temporal else 0)
         if pairs is None:
             pairs = torch.empty((max(16, 8 * n), 2), dtype=torch.int32, device=mn.device)
         for _ in range(2):

@@ -61,6 +61,17 @@ enum {
 /* Flags of the broadphase calls. */
 #define GSAP_FLAG_SORTED 0x1u /* output sorted by (i, j); otherwise any order */
 #define GSAP_FLAG_GRAPH 0x2u  /* run the pipeline as a cached CUDA graph */
+/* Temporal coherence for frame-to-frame calls: the call sweeps with the axes
+ * and cell grid computed from the previous call's input (a call of the same
+ * n, scene count, mode and settings on this handle) while its own PCA runs
+ * beside the sweep and prepares the next call's.  The reference likewise
+ * carries its sweep interval from one frame to the next (Sap.cpp:226-243).
+ * The pair set is exact either way (any grid gives the same pairs); what
+ * changes is the work: if the scene moved far since the previous call the
+ * stale grid costs time, and objects that grew a lot can exceed the entry
+ * capacity (GSAP_ERR_CAPACITY, after which the next call recomputes first).
+ * The first call, or one of a different shape, runs the plain pipeline. */
+#define GSAP_FLAG_TEMPORAL 0x4u
 
 typedef struct gsap_config {
     uint32_t mode;          /* GSAP_MODE_* used by gsap_broadphase_* (gsap_sap_collision is always sphere) */

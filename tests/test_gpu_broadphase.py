@@ -242,3 +242,29 @@ def test_bounded_wait_reports_timeout_and_recovers(cuda, oracle_lib):
     torch.cuda.synchronize()
     mn, mx = scenes.aabb_uniform(4096, 3)
     assert np.array_equal(run_bp(sap, mn, mx, cuda), oracle_lib.bf_aabb(mn, mx))
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_temporal_mode_is_exact_frame_to_frame(cuda, oracle_lib, graph):
+    """GSAP_FLAG_TEMPORAL: every call sweeps with the previous call's grid
+    while its own PCA runs beside it.  Jittered frames, a frame moved far
+    away, a frame of another size: the pair set is the brute force's each
+    time."""
+    from gsap_gb300 import Sap, scenes
+    n = 30_000
+    c, h, _ = scenes.aabb_gauss_parts(n, seed=31, std=(25.0, 6.0, 2.0))
+    sap = Sap(n + 1000)
+
+    def frame(cc, hh):
+        mn = np.concatenate([cc - hh, np.zeros((len(cc), 1), np.float32)], 1)
+        mx = np.concatenate([cc + hh, np.zeros((len(cc), 1), np.float32)], 1)
+        got = sap.broadphase(to_dev(mn, cuda), to_dev(mx, cuda), sorted=True, graph=graph, temporal=True)
+        assert np.array_equal(got.cpu().numpy().astype(np.uint32), oracle_lib.bf_aabb(mn, mx))
+
+    for k in range(4):
+        frame(scenes.jitter(c, seed=100 + k), h)
+    frame(c + np.float32([60.0, -20.0, 5.0]), h)    # far from the grid of the previous frame
+    frame(c[::-1].copy() * np.float32(1.5), h[::-1].copy())  # rescaled and renumbered
+    c2, h2, _ = scenes.aabb_gauss_parts(n + 1000, seed=32, std=(25.0, 6.0, 2.0))
+    frame(c2, h2)                                   # another size: plain pipeline first
+    frame(scenes.jitter(c2, seed=7), h2)
