@@ -45,7 +45,7 @@ struct Ctrl {
     uint32_t scan_total;      // total of the last look-back scan
     uint32_t scan_ctr;        // tile counter of the look-back scan
     uint32_t sort_n;          // key count of a standalone sort
-    uint32_t long_rows;       // canonical output: rows longer than the register sort
+    uint32_t long_rows;       // canonical output: rows queued for k_rowsort_long
     unsigned long long tests; // sweep: candidate pairs tested (diagnostics)
     unsigned long long iters; // sweep: warp iterations of the candidate loop (diagnostics)
     uint32_t hist[kMaxPasses][256];

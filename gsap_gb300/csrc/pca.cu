@@ -6,11 +6,14 @@
 // tree reductions over float4 arrays (the covariance rows pre-divided by n
 // and written to two 16n-byte temporaries) feed a <<<1,1>>> kernel that picks
 // the coordinate axis of largest variance.  Here one pass over the input
-// accumulates compensated (two-sum) FP32 sums of d = c - pilot, d d^T, h and
-// h h^T per 4096-object work item; the last work item of each scene combines
-// the partials in FP64 (fixed order: deterministic), solves the 3x3
-// eigenproblem by cyclic Jacobi in FP64 and chooses the sweep grid; the last
-// scene resets the counters of the later stages.
+// (k_pca) accumulates per 4096-object work item compensated (two-sum) FP32
+// sums of d = c - pilot and d d^T, and plain FP32 sums of the half extents h
+// and h h^T (they only size the grid); then one CTA per scene (k_pca_finish)
+// combines its partials in float-float arithmetic in a fixed order
+// (deterministic), forms the covariance in FP64, solves the 3x3 eigenproblem
+// (FP32 Jacobi refined in FP64, scene_math.cuh) and chooses the sweep grid;
+// the last scene lays out the keys and resets the counters of the later
+// stages.
 #include "internal.cuh"
 #include "scene_math.cuh"
 #include <math.h>
@@ -155,11 +158,13 @@ __global__ void __launch_bounds__(kThreads) k_pca(BpScratch S, BpArgs A) {
     }
 }
 
-// K1b: one CTA per scene combines the scene's partials in FP64 (fixed order:
-// deterministic), solves the 3x3 eigenproblem and picks the grid; the last
-// scene to finish computes the global bucket bases and the key layout and
-// resets the counters of the later stages.  A separate launch keeps the FP64
-// tail's registers out of the streaming kernel.
+// K1b: one CTA per scene combines the scene's partials (float-float, fixed
+// order: deterministic), solves the 3x3 eigenproblem and picks the grid; the
+// last scene to finish computes the global bucket bases and the key layout
+// and resets the counters of the later stages.  In temporal mode it writes
+// the next call's parameters instead and leaves the counters to the main
+// branch.  A separate launch keeps the FP64 tail's registers out of the
+// streaming kernel.
 __global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, uint64_t entry_cap, int temporal) {
     Scene* const out = temporal ? S.scenes_next : S.scenes;
     __shared__ uint32_t s_flag;
