@@ -688,7 +688,7 @@ extern "C" int gsap_debug_sizes(uint32_t* out) {
 
 gsap_status gsap::bp_both_async(gsap_sap* h, int mode, const float4* mn, const float4* mx, const uint32_t* off,
                                 uint32_t S, uint32_t n, uint2* pairs, uint64_t cap, int32_t* entries,
-                                uint64_t entry_cap, cudaStream_t st, BpDeviceCounts* out) {
+                                uint64_t entry_cap, cudaStream_t st, BpDeviceCounts* out, uint32_t flags) {
     gsap_status v = validate(h, (const float*)mn, (const float*)mx, n, mode, pairs, off ? S : 1);
     if (v != GSAP_OK) return v;
     if (out) {
@@ -709,6 +709,8 @@ gsap_status gsap::bp_both_async(gsap_sap* h, int mode, const float4* mn, const f
     c.entries = entries;
     c.ecap = entry_cap;
     c.both = 1;
+    c.flags = flags & GSAP_FLAG_TEMPORAL;
+    temporal_resolve(h, c);
     if (n < 2 && !off) {
         // empty list: zero the counts and row offsets the consumers read
         CK(cudaMemsetAsync(&h->s.ctrl->pair_count, 0, 8, st));

@@ -15,10 +15,11 @@ struct BpDeviceCounts {
 };
 
 // Both-direction canonical pair list (Sap::collision format, any predicate)
-// without any host synchronisation: the counts stay on the device.
+// without any host synchronisation: the counts stay on the device.  flags
+// may hold GSAP_FLAG_TEMPORAL (the step-to-step callers of the rigid body).
 gsap_status bp_both_async(gsap_sap* h, int mode, const float4* mn, const float4* mx, const uint32_t* scene_off,
                           uint32_t num_scenes, uint32_t n, uint2* pairs, uint64_t cap, int32_t* entries,
-                          uint64_t entry_cap, cudaStream_t st, BpDeviceCounts* out);
+                          uint64_t entry_cap, cudaStream_t st, BpDeviceCounts* out, uint32_t flags = 0);
 
 gsap_status set_error(gsap_status st, const char* msg);
 

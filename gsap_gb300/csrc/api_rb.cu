@@ -5,7 +5,10 @@
 // handle owns the SoA state in device memory; uploads are plain host->device
 // copies (the reference's GL pixel-buffer set-up, :88-98, is dropped: poses
 // are read back with gsap_rb_get_state instead).  gsap_rb_step runs a whole
-// step, broadphase included, without host synchronisation.
+// step, broadphase included, without host synchronisation; its broadphase
+// runs in temporal mode (GSAP_FLAG_TEMPORAL): the cell grid of the previous
+// step while this step's PCA runs beside the sweep.  The pair list is exact
+// either way.
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -303,7 +306,8 @@ extern "C" gsap_status gsap_rb_step(gsap_rb* h, gsap_sap* bp, float dt, void* st
         if ((r = gsap_rb_update_particle_data(h, stream)) != GSAP_OK) return r;
         BpDeviceCounts dc;
         r = bp_both_async(bp, GSAP_MODE_SPHERE, h->p_pos, nullptr, nullptr, 1, (uint32_t)h->n_particles,
-                          (uint2*)h->pairs, (uint64_t)h->max_pairs, h->entries, (uint64_t)h->max_particles, st, &dc);
+                          (uint2*)h->pairs, (uint64_t)h->max_pairs, h->entries, (uint64_t)h->max_particles, st, &dc,
+                          GSAP_FLAG_TEMPORAL);
         if (r != GSAP_OK) return r;
         if ((r = gsap_rb_prepare(h, stream)) != GSAP_OK) return r;
         RCK(rb_clear_force_ref(h->p_pos, h->p_vel, h->p_mass, h->p_force, h->cp.sp_multip, h->cp.dp_multip,
@@ -322,7 +326,7 @@ extern "C" gsap_status gsap_rb_step(gsap_rb* h, gsap_sap* bp, float dt, void* st
     RCK(rb_body_aabb(h->pos, h->p_rel, h->pstart, h->npart, h->bmin, h->bmax, h->n_bodies, st));
     BpDeviceCounts dc;
     r = bp_both_async(bp, GSAP_MODE_AABB, h->bmin, h->bmax, h->scene_off, h->num_scenes ? h->num_scenes : 1,
-                      (uint32_t)h->n_bodies, h->body_pairs, h->body_pair_cap, nullptr, 0, st, &dc);
+                      (uint32_t)h->n_bodies, h->body_pairs, h->body_pair_cap, nullptr, 0, st, &dc, GSAP_FLAG_TEMPORAL);
     if (r != GSAP_OK) return r;
     RCK(rb_forces_cfg(h->pos, h->p_rel, h->p_vel, h->p_body, h->pstart, h->npart, h->body_pairs, dc.rowoff,
                       h->body_pair_cap, p, h->p_force, h->n_particles, st));

@@ -283,7 +283,9 @@ float* gsap_rb_particle_force(gsap_rb* h);   /* getParticleForce */
  * Reference model: particle-sphere broadphase through `bp` in the
  * Sap::collision format.  Config model: body-AABB broadphase through `bp`
  * then particle contact between overlapping bodies (per scene when scenes
- * are set).  No host synchronisation inside the step. */
+ * are set).  No host synchronisation inside the step.  The broadphase runs
+ * with GSAP_FLAG_TEMPORAL (the previous step's cell grid; exact pairs either
+ * way), as the reference's step carries its sweep interval over. */
 gsap_status gsap_rb_step(gsap_rb* h, gsap_sap* bp, float dt, void* stream);
 
 /* Handle-owned arrays for gsap_rb_copy_out / gsap_rb_copy_in. */
