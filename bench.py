@@ -345,8 +345,8 @@ def run_ours(args, world, rank, local):
     if not args.no_extras:
         extras = run_extras(args, dev, stream)
 
-    # pca + finish, project, one per radix pass, sweep, scan, scatter, row sort (short and long rows)
-    launches_per_call = 8 + passes
+    # pca + finish, project, one per radix pass, sweep, row sums + row scan, scatter, rank, long rows
+    launches_per_call = 9 + passes
     clocks = clk.summary()
     line = {
         "metric": "1M-AABB PCA sweep-and-prune broadphase throughput (sorted i<j pair set)",

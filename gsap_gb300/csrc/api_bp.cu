@@ -120,7 +120,7 @@ static void free_scratch(gsap_sap* h) {
     BpScratch& s = h->s;
     void* ptrs[] = {s.ctrl, s.scenes, s.scenes_next, s.partials, s.scene_done, s.work_start, s.objcell, s.objscene,
                     s.keys[0], s.keys[1], s.vals[0], s.vals[1], s.status, s.rowcnt, s.rowoff, s.tmp_pairs,
-                    s.grp_pairs, s.tmp_rank, s.smin, s.smax, s.longrows};
+                    s.grp_pairs, s.tmp_rank, s.smin, s.smax, s.longrows, s.tile_sums};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (h->h_ctrl) cudaFreeHost(h->h_ctrl);
@@ -188,6 +188,7 @@ extern "C" gsap_sap* gsap_sap_create(uint32_t max_n, const gsap_config* cfg) {
     A((void**)&s.longrows, 4ull * (max_n + 1));
     A((void**)&s.rowcnt, 4ull * (max_n + 1));
     A((void**)&s.rowoff, 4ull * (max_n + 1));
+    A((void**)&s.tile_sums, 4ull * (max_n / 4096 + 2));
     A((void**)&s.tmp_pairs, 8ull * s.pair_cap_internal);
     A((void**)&s.grp_pairs, 16ull * s.pair_cap_internal);  // both-direction form: two entries per pair
     A((void**)&s.tmp_rank, 8ull * s.pair_cap_internal);

@@ -7,7 +7,7 @@
 // SapKernel.cu:2122-2360, :2802-2855).  The sweep emits every pair exactly
 // once and already counts pairs per row (first id, or both ids for the
 // both-direction format), so canonicalisation is a counting sort:
-//   1. exclusive look-back scan of the row counts -> row offsets;
+//   1. exclusive scan of the row counts -> row offsets (reduce, then scan);
 //   2. scatter each pair into its row(s) of an internal buffer at the slot
 //      the sweep drew from the row counter when it stored the pair (the
 //      scan has read the counters and put them back to zero for the next
@@ -163,6 +163,107 @@ __global__ void __launch_bounds__(kThreads) k_scan(BpScratch S, uint32_t* in, ui
     }
 }
 
+// Row offsets in two launches with no look-back chain (mode 0 of k_scan as
+// a reduce-then-scan): k_rowsum sums every 4096-count tile; k_rowscan adds
+// up the sums of the tiles before its own, scans its counts into the
+// offsets and puts the counters back to zero for the next call.
+__device__ __forceinline__ uint32_t cta_sum256(uint32_t v, uint32_t* s_w) {
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    v = __reduce_add_sync(0xffffffffu, v);
+    if (lane == 0) s_w[wid] = v;
+    __syncthreads();
+    uint32_t t = 0;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) t += s_w[w];
+    __syncthreads();
+    return t;
+}
+
+__global__ void __launch_bounds__(kThreads) k_rowsum(const uint32_t* __restrict__ in, uint32_t* tsum, uint32_t n) {
+    __shared__ uint32_t s_w[kThreads / 32];
+    const uint32_t b = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    uint32_t sum = 0;
+    if (b + kScanItems <= n) {
+        const uint4* src = reinterpret_cast<const uint4*>(in + b);
+#pragma unroll
+        for (int q = 0; q < kScanItems / 4; ++q) {
+            const uint4 x4 = src[q];
+            sum += x4.x + x4.y + x4.z + x4.w;
+        }
+    } else {
+        for (uint32_t i = b; i < n && i < b + kScanItems; ++i) sum += in[i];
+    }
+    const uint32_t t = cta_sum256(sum, s_w);
+    if (threadIdx.x == 0) tsum[blockIdx.x] = t;
+}
+
+__global__ void __launch_bounds__(kThreads) k_rowscan(uint32_t* in, uint32_t* out, const uint32_t* __restrict__ tsum,
+                                                      uint32_t n) {
+    __shared__ uint32_t s_w[kThreads / 32];
+    const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const uint32_t t = blockIdx.x;
+    // offset of this tile: the sums of all tiles before it
+    uint32_t ps = 0;
+    for (uint32_t k = tid; k < t; k += kThreads) ps += tsum[k];
+    const uint32_t tile_off = cta_sum256(ps, s_w);
+    const uint32_t b = t * kScanTile + tid * kScanItems;
+    uint32_t v[kScanItems];
+    const bool full = b + kScanItems <= n;
+    if (full) {
+        uint4* src = reinterpret_cast<uint4*>(in + b);
+#pragma unroll
+        for (int q = 0; q < kScanItems / 4; ++q) {
+            const uint4 x4 = src[q];
+            v[4 * q] = x4.x; v[4 * q + 1] = x4.y; v[4 * q + 2] = x4.z; v[4 * q + 3] = x4.w;
+            src[q] = make_uint4(0u, 0u, 0u, 0u);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            const uint32_t i = b + k;
+            v[k] = i < n ? in[i] : 0u;
+            if (i < n) in[i] = 0u;
+        }
+    }
+    uint32_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) sum += v[k];
+    uint32_t x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) s_w[wid] = x;
+    __syncthreads();
+    uint32_t pre = 0, tot = 0;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) {
+        if ((uint32_t)w < wid) pre += s_w[w];
+        tot += s_w[w];
+    }
+    uint32_t run = tile_off + pre + x - sum;
+    if (t == gridDim.x - 1 && tid == 0) out[n] = tile_off + tot;
+    if (full) {
+        uint4* dst = reinterpret_cast<uint4*>(out + b);
+#pragma unroll
+        for (int q = 0; q < kScanItems / 4; ++q) {
+            uint4 o4;
+            o4.x = run; run += v[4 * q];
+            o4.y = run; run += v[4 * q + 1];
+            o4.z = run; run += v[4 * q + 2];
+            o4.w = run; run += v[4 * q + 3];
+            dst[q] = o4;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            if (b + k < n) out[b + k] = run;
+            run += v[k];
+        }
+    }
+}
+
 // Scatter pairs into their rows at the slots the sweep drew.  both: row i
 // gets (i, j) and row j (j, i).  No atomics.
 __global__ void __launch_bounds__(kThreads) k_scatter(BpScratch S, const uint2* __restrict__ in, uint64_t in_cap,
@@ -293,7 +394,9 @@ cudaError_t launch_canonical(const BpScratch& s, uint32_t n, const uint2* in_pai
                              uint2* out_pairs, uint64_t out_cap, int both, int32_t* entries, uint64_t entry_cap,
                              uint32_t spin, cudaStream_t st) {
     const int grid = sm_count() * 4;
-    k_scan<0><<<grid, kThreads, 0, st>>>(s, s.rowcnt, s.rowoff, nullptr, 0, n, 5, spin);
+    const uint32_t ntiles = (n + kScanTile - 1) / kScanTile;
+    k_rowsum<<<ntiles, kThreads, 0, st>>>(s.rowcnt, s.tile_sums, n);
+    k_rowscan<<<ntiles, kThreads, 0, st>>>(s.rowcnt, s.rowoff, s.tile_sums, n);
     const uint64_t grp_cap = 2 * s.pair_cap_internal;
     k_scatter<<<sm_count() * 16, kThreads, 0, st>>>(s, in_pairs, in_cap, s.grp_pairs, grp_cap, both);
     k_rank<<<sm_count() * 8, kThreads, 0, st>>>(s, s.grp_pairs, grp_cap, n, out_pairs, out_cap);

@@ -104,6 +104,7 @@ struct BpScratch {
     uint32_t* longrows;        // canonical output: ids of rows placed by k_rowsort_long
     uint32_t* rowcnt;          // per object pair counts (canonical output)
     uint32_t* rowoff;          // exclusive offsets, n+1
+    uint32_t* tile_sums;       // row-count sums per 4096-row tile (canonical output)
     uint32_t* tmp_pairs;       // unsorted pairs before canonicalisation
     uint2* grp_pairs;          // pairs grouped by row, before the in-row order (canonical output)
     uint32_t* tmp_rank;        // per unsorted pair k: its slot in row first (rank[k]); both-direction
