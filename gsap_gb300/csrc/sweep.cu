@@ -149,8 +149,10 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
             float t = __fmul_rn(__fsub_rn(h1, sc->q_org), sc->q_scale);
             uint32_t qh = (uint32_t)fminf(fmaxf(t, 0.f), qmax);
             const uint32_t kb = (key & ~qmask) | qh;  // >= key: q(hi1) >= q(lo1)
-            // last index with key <= kb: gallop from e, then bisect (lo: key <= kb, hi: key > kb or E)
-            uint32_t lo = e, hi = E, step = 1;
+            // last index with key <= kb: gallop from e with a first step near
+            // the typical run length (tens of entries), then bisect
+            // (lo: key <= kb, hi: key > kb or E)
+            uint32_t lo = e, hi = E, step = 16;
             while (true) {
                 if (step >= E - lo) break;
                 const uint32_t p = lo + step;
