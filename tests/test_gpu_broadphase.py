@@ -268,3 +268,36 @@ def test_temporal_mode_is_exact_frame_to_frame(cuda, oracle_lib, graph):
     c2, h2, _ = scenes.aabb_gauss_parts(n + 1000, seed=32, std=(25.0, 6.0, 2.0))
     frame(c2, h2)                                   # another size: plain pipeline first
     frame(scenes.jitter(c2, seed=7), h2)
+
+
+def test_batched_temporal_frames_are_exact(cuda, oracle_lib):
+    """GSAP_FLAG_TEMPORAL on batched calls: each scene's pairs stay the brute
+    force's from frame to frame, including a frame where scene sizes change
+    (same total and count) and a frame where one scene moves far away."""
+    import torch
+    from gsap_gb300 import Sap, scenes
+    mn, mx, off = scenes.batched_aabb(S=16, seed=12, lo=16, hi=2500)
+    n = len(mn)
+    bsap = Sap(n, max_scenes=16)
+
+    def frame(a, b, o):
+        got = bsap.broadphase_batched(to_dev(a, cuda), to_dev(b, cuda), torch.from_numpy(o.astype(np.int32)).to(cuda),
+                                      temporal=True).cpu().numpy().astype(np.uint32)
+        want = [oracle_lib.bf_aabb(a[s:e], b[s:e]).astype(np.int64) + s for s, e in zip(o[:-1], o[1:]) if e - s >= 2]
+        assert np.array_equal(got, np.concatenate(want).astype(np.uint32))
+
+    rng = np.random.default_rng(1)
+    for k in range(3):
+        d = rng.normal(0, 0.05, (n, 3)).astype(np.float32)
+        a, b = mn.copy(), mx.copy()
+        a[:, :3] += d
+        b[:, :3] += d
+        frame(a, b, off)
+    off2 = off.copy()
+    off2[5] = (off[4] + off[6]) // 2  # scene edges move, same count and total
+    frame(mn, mx, off2)
+    a, b = mn.copy(), mx.copy()
+    s, e = int(off2[7]), int(off2[8])
+    a[s:e, :3] += 500.0
+    b[s:e, :3] += 500.0
+    frame(a, b, off2)
