@@ -393,6 +393,7 @@ static gsap_status finish(gsap_sap* h, cudaStream_t st, uint64_t* count_out, uin
         if (err & kErrEntryCap) return fail(GSAP_ERR_CAPACITY, "sweep entries exceeded the handle's capacity (raise entry_factor)");
         if (err & kErrCellRange) return fail(GSAP_ERR_CAPACITY, "too many sweep cells for the key width");
         if (err & kErrPairCap) return fail(GSAP_ERR_CAPACITY, "pairs exceeded an output capacity");
+        if (err & kErrOffsets) return fail(GSAP_ERR_INVALID, "scene offsets must run from 0 to n and never decrease");
         if (err & kErrInternal) return fail(GSAP_ERR_CUDA, "internal consistency check failed (device error word 0x%x)", err);
         return fail(GSAP_ERR_CUDA, "device error word 0x%x", err);
     }

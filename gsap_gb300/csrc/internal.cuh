@@ -20,6 +20,7 @@ enum : uint32_t {
     kErrNonFinite = 8u,    // NaN / Inf in the input bounds
     kErrCellRange = 16u,   // internal: grid wider than 65535 cells per axis
     kErrInternal = 32u,    // an internal consistency check failed (index out of range)
+    kErrOffsets = 64u,     // batched scene offsets not 0 .. n non-decreasing
 };
 
 // Look-back status word: [63:32] tag, [31:30] flag, [29:0] value.
@@ -255,11 +256,15 @@ __device__ __forceinline__ void kahan_merge(float& hi, float& lo, float hi2, flo
 // ------------------------------------------------------------- work plan
 #ifdef __CUDACC__
 
+// Scene s covers objects [scene_begin, scene_end).  The caller's offsets are
+// clamped into [0, n] and made non-decreasing here, so no kernel can index
+// outside the input whatever the offsets hold; k_plan reports offsets that
+// needed clamping (GSAP_ERR_INVALID).
 __device__ __forceinline__ uint32_t scene_begin(const BpArgs& A, uint32_t s) {
-    return A.scene_off ? A.scene_off[s] : 0u;
+    return A.scene_off ? min(A.scene_off[s], A.n) : 0u;
 }
 __device__ __forceinline__ uint32_t scene_end(const BpArgs& A, uint32_t s) {
-    return A.scene_off ? A.scene_off[s + 1] : A.n;
+    return A.scene_off ? min(max(A.scene_off[s + 1], scene_begin(A, s)), A.n) : A.n;
 }
 __device__ __forceinline__ uint32_t work_items(uint32_t n_s) {
     return n_s == 0 ? 1u : (n_s + kChunk - 1) / kChunk;
@@ -287,7 +292,7 @@ __device__ __forceinline__ bool map_work(uint32_t w, const BpScratch& S, const B
     scene = lo;
     wfirst = S.work_start[lo];
     nw = S.work_start[lo + 1] - wfirst;
-    uint32_t sb = A.scene_off[lo], se = A.scene_off[lo + 1];
+    uint32_t sb = scene_begin(A, lo), se = scene_end(A, lo);
     b = sb + (w - wfirst) * kChunk;
     e = min(se, b + kChunk);
     return true;

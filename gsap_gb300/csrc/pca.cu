@@ -30,7 +30,13 @@ __global__ void __launch_bounds__(1024) k_plan(BpScratch S, BpArgs A) {
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (uint32_t base = 0; base < A.num_scenes; base += 1024) {
         uint32_t s = base + threadIdx.x;
-        uint32_t v = s < A.num_scenes ? work_items(A.scene_off[s + 1] - A.scene_off[s]) : 0u;
+        uint32_t v = 0;
+        if (s < A.num_scenes) {
+            v = work_items(scene_end(A, s) - scene_begin(A, s));
+            const bool bad = A.scene_off[s + 1] < A.scene_off[s] || (s == 0 && A.scene_off[0] != 0u) ||
+                             (s + 1 == A.num_scenes && A.scene_off[s + 1] != A.n);
+            if (bad) atomicOr(&S.ctrl->error, kErrOffsets);
+        }
         uint32_t x = v;
         for (int o = 1; o < 32; o <<= 1) {
             uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
@@ -173,7 +179,10 @@ __global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, 
     if (scene >= A.num_scenes) return;
     const uint32_t sb = scene_begin(A, scene), se = scene_end(A, scene);
     const uint32_t wfirst = A.scene_off ? S.work_start[scene] : 0u;
-    const uint32_t nw = A.scene_off ? S.work_start[scene + 1] - wfirst : work_items(A.n);
+    // (bad offsets can plan more work items than were launched: only
+    // partials that k_pca wrote are read)
+    const uint32_t nw0 = A.scene_off ? S.work_start[scene + 1] - wfirst : work_items(A.n);
+    const uint32_t nw = wfirst < A.num_work ? min(nw0, A.num_work - wfirst) : 0u;
     // Combine the scene's partials in float-float (two-sum) arithmetic on the
     // FP32 pipes: thread t merges items t, t+256, ..., then warps and the CTA
     // merge in a fixed order (deterministic); only the final hi + lo pairs go

@@ -301,3 +301,22 @@ def test_batched_temporal_frames_are_exact(cuda, oracle_lib):
     a[s:e, :3] += 500.0
     b[s:e, :3] += 500.0
     frame(a, b, off2)
+
+
+def test_bad_scene_offsets_are_reported(cuda, oracle_lib):
+    """Offsets that decrease, or do not run from 0 to n, are clamped on the
+    device (no access outside the input) and reported as GSAP_ERR_INVALID;
+    the handle then serves a valid call."""
+    import torch
+    from gsap_gb300 import GsapError, Sap, scenes
+    mn, mx, off = scenes.batched_aabb(S=4, seed=2, lo=100, hi=400)
+    n = len(mn)
+    bsap = Sap(n, max_scenes=4)
+    dmn, dmx = to_dev(mn, cuda), to_dev(mx, cuda)
+    for bad in ([0, 300, 200, 350, n], [0, 100, 200, 300, n + 50], [5, 100, 200, 300, n]):
+        with pytest.raises(GsapError) as ei:
+            bsap.broadphase_batched(dmn, dmx, torch.tensor(bad, dtype=torch.int32, device=cuda))
+        assert ei.value.status == 1  # GSAP_ERR_INVALID
+    got = bsap.broadphase_batched(dmn, dmx, torch.from_numpy(off.astype(np.int32)).to(cuda))
+    want = [oracle_lib.bf_aabb(mn[a:b], mx[a:b]).astype(np.int64) + a for a, b in zip(off[:-1], off[1:])]
+    assert np.array_equal(got.cpu().numpy().astype(np.uint32), np.concatenate(want).astype(np.uint32))
