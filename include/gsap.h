@@ -135,8 +135,10 @@ gsap_status gsap_broadphase_aabb(gsap_sap* h, const float* d_min, const float* d
  * [d_scene_offsets[s], d_scene_offsets[s+1]) of d_min / d_max (device array
  * of S+1 uint32, d_scene_offsets[0] = 0, d_scene_offsets[S] = n).  Pairs
  * (i, j), i < j, use global object ids and never cross a scene.  One launch
- * per pipeline stage for all scenes.  No reference counterpart (the
- * reference handles one scene per Sap object). */
+ * per pipeline stage for all scenes.  Offsets that decrease or do not run
+ * from 0 to n are clamped on the device (nothing outside the input is read)
+ * and reported as GSAP_ERR_INVALID when the call's status is read.  No
+ * reference counterpart (the reference handles one scene per Sap object). */
 gsap_status gsap_broadphase_batched(gsap_sap* h, const float* d_min, const float* d_max,
                                     const uint32_t* d_scene_offsets, uint32_t num_scenes, uint32_t n,
                                     uint32_t* d_pairs, uint64_t pair_cap,
