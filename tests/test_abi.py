@@ -123,3 +123,26 @@ def test_grid_respects_entry_bound(gsap_lib):
         w2, w3 = 2 * np.abs(U[1]) @ h[0], 2 * np.abs(U[2]) @ h[0]
         worst = min(G2, w2 / s2 + 2) * min(G3, w3 / s3 + 2) * len(pts)
         assert worst <= 8 * len(pts) + 4096
+
+
+def test_demo_scene_and_snapshot_round_trip(tmp_path):
+    """The headless demo's scene (DemoParticles::init layout) and its binary
+    snapshots; no GPU needed."""
+    from gsap_gb300 import demo
+    sc = demo.demo_scene(512, n_row=8, seed=3)
+    assert sc["pos"].shape == (512, 4) and sc["n_particles"] == 6 * 512
+    assert np.array_equal(sc["shape_idx"][:4], [0, 1, 0, 1])
+    # hexagon offsets: six particles at one radius from the body centre
+    r0 = np.linalg.norm(sc["ref_pos"][0:6, :3], axis=1)
+    r1 = np.linalg.norm(sc["ref_pos"][10:16, :3], axis=1)
+    assert np.allclose(r0, 0.5005) and np.allclose(r1, 0.5005 * 1.2)
+    assert sc["pos"][:, 1].min() == np.float32(3.6) and sc["pos"][:, 1].max() == np.float32(3.6 * 8)
+    state = {k: sc[k] + 1.0 for k in ("pos", "quat", "lin_vel", "ang_vel")}
+    path = tmp_path / "snap.npz"
+    demo.save_snapshot(path, sc, state, step=7)
+    back, step = demo.load_snapshot(path)
+    assert step == 7 and back["n_particles"] == sc["n_particles"]
+    for k in ("pos", "quat", "lin_vel", "ang_vel"):
+        assert np.array_equal(back[k], state[k])
+    for k in ("shape_idx", "p_start", "ref_pos", "shape_inv_inertia"):
+        assert np.array_equal(back[k], sc[k])

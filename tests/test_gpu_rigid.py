@@ -156,3 +156,27 @@ def test_batched_config_scenes_stay_separate(cuda, oracle_lib):
     g = prb.get_state()
     assert relerr(g["pos"][:, :3], st64["pos"][:, :3]) <= REL_TOL
     assert relerr(g["lin_vel"][:, :3], st64["lin_vel"][:, :3]) <= REL_TOL
+
+
+def test_headless_demo_runs_and_restarts_from_snapshot(cuda, tmp_path):
+    """The DemoParticles scene stepped headless; a run restarted from a
+    binary snapshot continues like the uninterrupted one."""
+    from gsap_gb300 import demo
+    sc = demo.demo_scene(512, n_row=8, seed=1)
+    d = demo.Demo(sc)
+    d.run(30)
+    st = d.state()
+    assert all(np.isfinite(st[k]).all() for k in st)
+    assert st["pos"][:, 1].mean() < sc["pos"][:, 1].mean() - 0.5  # falling under gravity
+    path = tmp_path / "snap.npz"
+    demo.save_snapshot(path, sc, st, d.steps)
+    d.run(10)
+    a = d.state()
+    d.sap.check()
+    sc2, step = demo.load_snapshot(path)
+    assert step == 30
+    d2 = demo.Demo(sc2)
+    d2.run(10)
+    b = d2.state()
+    for k in ("pos", "lin_vel"):
+        assert relerr(b[k][:, :3], a[k][:, :3]) < 1e-4, k
