@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_onesweep(BpScratch S, const uin
     __shared__ uint32_t s_start[256];
     __shared__ uint32_t s_gb[256];
     __shared__ uint32_t s_scan[8];
-    __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_tile, s_tile_next;
     const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const uint32_t n = min(*count_ptr, cap);
     const uint32_t ntiles = (n + TILE - 1) / TILE;
@@ -62,31 +62,33 @@ __global__ void __launch_bounds__(kThreads, 2) k_onesweep(BpScratch S, const uin
     const uint32_t lt = lanemask_lt();
 
     s_gdig[tid] = cta_excl_scan256(S.ctrl->hist[pass][tid], s_scan);
-
-    while (true) {
-        if (tid == 0) s_tile = atomicAdd(&S.ctrl->tile_ctr[pass], 1u);
+    if (tid == 0) s_tile = atomicAdd(&S.ctrl->tile_ctr[pass], 1u);
 #pragma unroll
-        for (int w = 0; w < kThreads / 32; ++w) s_wh[w][tid] = 0u;
-        s_next[tid] = 0u;
-        __syncthreads();
-        const uint32_t t = s_tile;
-        if (t >= ntiles) break;
+    for (int w = 0; w < kThreads / 32; ++w) s_wh[w][tid] = 0u;
+    s_next[tid] = 0u;
+    __syncthreads();
+    uint32_t t = s_tile;
+    // The keys and values of the CTA's next tile are loaded while it waits in
+    // the look-back of the current one (tickets are taken in order, so every
+    // tile a CTA waits on belongs to a running CTA).
+    uint32_t key[ITEMS], val[ITEMS];
+    auto load_tile = [&](uint32_t tt) {
+        const uint32_t wb0 = tt * TILE + wid * 32 * ITEMS;
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            const uint32_t idx = wb0 + k * 32 + lane;
+            const bool in = tt < ntiles && idx < n;
+            key[k] = in ? __ldcs(kin + idx) : 0u;
+            val[k] = in ? __ldcs(vin + idx) : 0u;
+        }
+    };
+    load_tile(t);
+    while (t < ntiles) {
         const uint32_t tbase = t * TILE;
         const uint32_t wb = tbase + wid * 32 * ITEMS;
         uint32_t tot = 0;
         {
-            uint32_t key[ITEMS], val[ITEMS], rk[ITEMS];
-#pragma unroll
-            for (int k = 0; k < ITEMS; ++k) {
-                uint32_t idx = wb + k * 32 + lane;
-                if (idx < n) {
-                    key[k] = __ldcs(kin + idx);
-                    val[k] = __ldcs(vin + idx);
-                } else {
-                    key[k] = 0u;
-                    val[k] = 0u;
-                }
-            }
+            uint32_t rk[ITEMS];
             // warp-level multi-split ranking, items in index order
 #pragma unroll
             for (int k = 0; k < ITEMS; ++k) {
@@ -115,9 +117,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_onesweep(BpScratch S, const uin
             }
             // publish the aggregates before anything else
             st_lb_u64(S.status + (uint64_t)t * 256u + tid, lb_word(tag, t == 0 ? kFlagPrefix : kFlagAgg, tot));
+            if (tid == 0) s_tile_next = atomicAdd(&S.ctrl->tile_ctr[pass], 1u);
             s_start[tid] = cta_excl_scan256(tot, s_scan);
-            __syncthreads();  // every digit's tile start is read below by other threads
-            // stage the tile in digit order (frees the registers for the look-back)
+            __syncthreads();  // every digit's tile start (and the next ticket) is read below
+            // stage the tile in digit order (frees the registers for the next tile)
 #pragma unroll
             for (int k = 0; k < ITEMS; ++k) {
                 if (wb + k * 32 + lane < n) {
@@ -132,6 +135,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_onesweep(BpScratch S, const uin
                 }
             }
         }
+        const uint32_t t_next = s_tile_next;
+        load_tile(t_next);  // in flight during the look-back and the write-out
         uint32_t excl = 0;
         if (t > 0) {
             excl = lookback(S.status, t, tid, 256u, tag, spin, &S.ctrl->error);
@@ -176,7 +181,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_onesweep(BpScratch S, const uin
                 }
             }
         }
+        __syncthreads();  // s_k / s_v / s_wh / s_next are reused by the next tile
+#pragma unroll
+        for (int w = 0; w < kThreads / 32; ++w) s_wh[w][tid] = 0u;
+        s_next[tid] = 0u;
         __syncthreads();
+        t = t_next;
     }
 }
 
