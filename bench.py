@@ -393,6 +393,36 @@ def run_extras(args, dev, stream):
 
     from gsap_gb300 import CONTACT_CONFIG, ParticleRigidBody, Sap, scenes
     out = {}
+    # --- small case: 16,384 AABBs, centres U[0,100]^3, half-extents U[0.1,0.5];
+    # the reference's own CPU path for it is the O(n^2) brute force
+    smn, smx = scenes.aabb_uniform(16384, 0)
+    dsmn, dsmx = torch.from_numpy(smn).to(dev), torch.from_numpy(smx).to(dev)
+    ssap = Sap(16384)
+    spairs = torch.empty((16 * 16384, 2), dtype=torch.int32, device=dev)
+    scnt = torch.zeros(1, dtype=torch.int64, device=dev)
+    for _ in range(5):
+        ssap.broadphase_async(dsmn, dsmx, spairs, scnt, sorted=True, graph=True, stream=stream)
+    torch.cuda.synchronize()
+    ssap.check()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(200):
+        ssap.broadphase_async(dsmn, dsmx, spairs, scnt, sorted=True, graph=True, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ssap.check()
+    small = {"n": 16384, "pairs": int(scnt.item()), "ms_per_call": round(e0.elapsed_time(e1) / 200, 4)}
+    if not args.no_cpu:
+        import oracle
+        oracle.build()
+        t0 = time.perf_counter()
+        bf = oracle.bf_aabb(smn, smx)
+        small["cpu_brute_force_ms"] = round((time.perf_counter() - t0) * 1e3, 2)
+        small["cpu_cores"] = os.cpu_count()
+        small["equal_to_brute_force"] = bool(np.array_equal(spairs[: len(bf)].cpu().numpy().astype(np.uint32), bf)
+                                             and int(scnt.item()) == len(bf))
+    out["small_16k"] = small
+    del ssap, spairs
     # --- batched broadphase: 4096 scenes, sizes log-uniform in [64, 65536]
     S = args.scenes
     mn, mx, off = scenes.batched_aabb(S=S, seed=7)
