@@ -320,3 +320,26 @@ def test_bad_scene_offsets_are_reported(cuda, oracle_lib):
     got = bsap.broadphase_batched(dmn, dmx, torch.from_numpy(off.astype(np.int32)).to(cuda))
     want = [oracle_lib.bf_aabb(mn[a:b], mx[a:b]).astype(np.int64) + a for a, b in zip(off[:-1], off[1:])]
     assert np.array_equal(got.cpu().numpy().astype(np.uint32), np.concatenate(want).astype(np.uint32))
+
+
+def test_degenerate_and_far_from_origin_scenes(cuda, oracle_lib):
+    """All boxes identical (zero spread: the eigensolve's degenerate path, one
+    cell, every pair overlapping), a flat scene (zero spread on one axis) and
+    a cloud a million units from the origin (FP32 spacing ~0.06 there)."""
+    from gsap_gb300 import Sap
+    rng = np.random.default_rng(17)
+    n = 300
+    same = np.tile(np.float32([[1.0, 2.0, 3.0, 0.0]]), (n, 1))
+    sap = Sap(4000, pair_factor=200)
+    got = run_bp(sap, same - np.float32([0.5, 0.5, 0.5, 0]), same + np.float32([0.5, 0.5, 0.5, 0]), cuda)
+    assert len(got) == n * (n - 1) // 2
+    c = rng.uniform(0, 30, (4000, 3)).astype(np.float32)
+    c[:, 2] = 7.0  # flat
+    h = rng.uniform(0.1, 0.6, (4000, 3)).astype(np.float32)
+    mn = np.concatenate([c - h, np.zeros((4000, 1), np.float32)], 1)
+    mx = np.concatenate([c + h, np.zeros((4000, 1), np.float32)], 1)
+    assert np.array_equal(run_bp(sap, mn, mx, cuda), oracle_lib.bf_aabb(mn, mx))
+    far = (rng.uniform(0, 40, (4000, 3)) + 1.0e6).astype(np.float32)
+    mn = np.concatenate([far - h, np.zeros((4000, 1), np.float32)], 1)
+    mx = np.concatenate([far + h, np.zeros((4000, 1), np.float32)], 1)
+    assert np.array_equal(run_bp(sap, mn, mx, cuda), oracle_lib.bf_aabb(mn, mx))
