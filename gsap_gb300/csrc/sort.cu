@@ -10,8 +10,9 @@
 // (eight ballots give every lane the mask of lanes holding the same digit),
 // publishes its per-digit counts, and finds its global offsets by a
 // decoupled look-back over earlier tiles (one thread per digit, eight
-// predecessor words per round trip).  Tiles are handed out in order by an atomic counter, so a tile only ever waits on
-// tiles that running CTAs own; every wait is bounded and reports
+// predecessor words per round trip) while the keys of its next tile load.
+// Tiles are handed out in order by an atomic counter, so a tile only ever
+// waits on tiles that running CTAs own; every wait is bounded and reports
 // GSAP_ERR_DEVICE_TIMEOUT instead of hanging.  Stable: equal digits keep
 // their input order, so the passes give the order of a stable sort.
 #include "internal.cuh"

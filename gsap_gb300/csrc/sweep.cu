@@ -8,9 +8,10 @@
 // second blocking read and the compaction assemPairsSphereSub :1649-1695),
 // and the cross pass of SapKernel.cu:2364-2446.
 //
-// Persistent warps take 32 consecutive sorted entries at a time from an
-// atomic counter (work stealing).  For its entry e a lane first finds, by a
-// galloping then binary search over the sorted keys, the end of the run of
+// Persistent warps take 128 consecutive sorted entries at a time from an
+// atomic counter (work stealing) and handle them in chunks of 32.  For its
+// entry e a lane first finds, by a galloping then binary search over the
+// sorted keys, the end of the run of
 // entries with key <= (bucket | q(hi1)): the q map is monotone, so these are
 // exactly the later entries of the same cell whose interval on u1 can meet
 // e's, and the run stops at the cell (and scene) boundary by construction.
@@ -31,9 +32,10 @@
 // needed.  With the per-entry owner flags of the gather (is this cell the
 // object's lowest on u2 / on u3) the rule is (f_i | f_j) == 3.  Object index
 // and flags travel inside the two 16-byte bound records, so a test makes
-// no load that depends on another.  Hits are
-// compacted through a per-warp shared-memory buffer that reserves global
-// space with one atomic per up to 128 pairs.
+// no load that depends on another.  Hits are compacted through a per-warp
+// shared-memory buffer that reserves global space with one atomic per up to
+// 128 pairs; for the canonical output every stored pair also draws its slot
+// in its row from the row counters.
 #include "internal.cuh"
 
 namespace gsap {
