@@ -30,8 +30,9 @@ constexpr uint32_t kValMask = (1u << 30) - 1u;
 
 // Control block: counters shared by the stages of one call.  Counters that a
 // stage consumes are reset by the stage that runs before it (the PCA
-// kernel's last CTA resets the projection/sort/sweep counters), or by their
-// own last user (per-scene PCA counters), so that no memset runs per call.
+// finish's last CTA resets the projection/sort/sweep counters; in temporal
+// mode k_reset does), or by their own last user (per-scene PCA counters, the
+// row counters zeroed by the row scan), so that no memset runs per call.
 struct Ctrl {
     uint32_t error;
     uint32_t epoch;           // ++ once per pipeline run; tags look-back words
