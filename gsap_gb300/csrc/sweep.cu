@@ -194,14 +194,15 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
         __syncwarp();
         tests += total;
         uint32_t before = 0;  // runs that start before the current window
-        for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+        // whole steps need no bound check; the last, partial step does
+        auto step = [&](const uint32_t t0, const bool full) {
             ++steps;
             const uint32_t d = start - t0;
             const uint32_t starts = __reduce_or_sync(0xffffffffu, (run > 0 && d < 32u) ? (1u << d) : 0u);
             const uint32_t t = t0 + lane;
             bool hit = false;
             uint32_t o = 0, oi = 0;
-            if (t < total) {
+            if (full || t < total) {
                 const uint32_t m = before + __popc(starts & le) - 1u;  // run of test t
                 const float4 ea = s_t0[wid][m], eb = s_t1[wid][m];
                 const uint32_t j = __float_as_uint(MODE == 0 ? ea.w : eb.x) + t;
@@ -238,7 +239,10 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
                 if (hit) s_buf[wid][nbuf + __popc(hm & lt)] = make_uint2(min(oi, o), max(oi, o));
                 nbuf += cnt;
             }
-        }
+        };
+        uint32_t t0 = 0;
+        for (; t0 + 32u <= total; t0 += 32u) step(t0, true);
+        if (t0 < total) step(t0, false);
         __syncwarp();  // the next chunk overwrites the run table
     }
     flush();
