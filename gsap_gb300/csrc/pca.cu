@@ -238,13 +238,17 @@ __global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, 
         Scene sc;
         choose_scene(z, A, entry_cap, A.n, sc);
         out[scene] = sc;
-        __threadfence();
-        uint32_t old = atomicAdd(&C->scenes_done, 1u);
-        s_flag = (old == A.num_scenes - 1) ? 1u : 0u;
+        if (A.num_scenes == 1) {
+            s_flag = 1u;  // the only scene: this CTA is the last one
+        } else {
+            __threadfence();
+            uint32_t old = atomicAdd(&C->scenes_done, 1u);
+            s_flag = (old == A.num_scenes - 1) ? 1u : 0u;
+        }
     }
     __syncthreads();
     if (!s_flag) return;
-    __threadfence();
+    if (A.num_scenes > 1) __threadfence();  // the other scenes' records are read below
     // Last scene: global bucket bases, key layout, and counter reset.
     __shared__ uint32_t s_wsum[kThreads / 32];
     __shared__ uint32_t s_carry;
