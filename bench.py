@@ -176,7 +176,7 @@ def run_ours(args, world, rank, local):
     d_count = torch.zeros(1, dtype=torch.int64, device=dev)
     stream = torch.cuda.current_stream()
     # autotuner (set-up, untimed): key width and cell factor for this input
-    tuned = None if fixed else sap.autotune(*dsets[0], pairs=pairs, sorted=True, graph=True, reps=3, stream=stream)
+    tuned = None if fixed else sap.autotune(*dsets[0], pairs=pairs, sorted=True, graph=True, reps=10, stream=stream)
     passes = (tuned["sort_bits"] if tuned else (args.sort_bits or 32)) // 8
 
     def call(k, sorted_=True, graph=True):
