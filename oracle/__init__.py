@@ -55,7 +55,8 @@ def lib():
         L.orc_bf_sphere.restype = C.c_int64
         L.orc_sap_ref.argtypes = [C.c_int, P, P, C.c_uint32, P, C.c_int64, C.c_int]
         L.orc_sap_ref.restype = C.c_int64
-        L.orc_sap_ref_sampled.argtypes = [C.c_int, P, P, C.c_uint32, C.c_uint32, P, C.c_int64, C.c_int]
+        L.orc_sap_ref_sampled.argtypes = [C.c_int, P, P, C.c_uint32, C.c_uint32, C.c_uint32, P, C.c_int64,
+                                          C.c_int, P]
         L.orc_sap_ref_sampled.restype = C.c_int64
         L.orc_both_directions.argtypes = [P, C.c_int64, P, P]
         L.orc_both_directions.restype = C.c_int64
@@ -123,22 +124,28 @@ def bf_sphere(spheres, threads=0):
     return _run_pairs(lambda a, p, c: L.orc_bf_sphere(a, C.c_uint32(len(s)), p, c, threads), _ptr(s))
 
 
-def sap_ref(mode, mn, mx=None, threads=0):
-    """The reference SaP algorithm restated on the CPU (mode 0 AABB, 1 sphere)."""
+def sap_ref(mode, mn, mx=None, threads=0, cap=None):
+    """The reference SaP algorithm restated on the CPU (mode 0 AABB, 1 sphere).
+    `cap` sizes the first output buffer; a call that finds more pairs runs
+    again with room for all of them."""
     mn = _f4(mn)
     mx = _f4(mx) if mx is not None else None
     L = lib()
     return _run_pairs(lambda a, b, p, c: L.orc_sap_ref(mode, a, b, C.c_uint32(len(mn)), p, c, threads),
-                      _ptr(mn), _ptr(mx))
+                      _ptr(mn), _ptr(mx), cap=cap)
 
 
-def sap_ref_sampled(mode, mn, mx, stride, threads=0):
-    """orc_sap_ref with the sweep started from every stride-th object only."""
+def sap_ref_sampled(mode, mn, mx, parts, part, threads=0):
+    """One call of orc_sap_ref with the sweeps started from slice `part` of
+    `parts` contiguous slices of each sorted group, keeping no pairs:
+    (pair count, seconds of the fixed stages, seconds of the stages that
+    scale with the sweep starts)."""
     mn = _f4(mn)
     mx = _f4(mx) if mx is not None else None
-    L = lib()
-    return _run_pairs(lambda a, b, p, c: L.orc_sap_ref_sampled(mode, a, b, C.c_uint32(len(mn)), C.c_uint32(stride),
-                                                               p, c, threads), _ptr(mn), _ptr(mx))
+    secs = np.zeros(2, np.float64)
+    npairs = lib().orc_sap_ref_sampled(mode, _ptr(mn), _ptr(mx), C.c_uint32(len(mn)), C.c_uint32(parts),
+                                       C.c_uint32(part), None, _i64(0), threads, _ptr(secs))
+    return int(npairs), float(secs[0]), float(secs[1])
 
 
 def both_directions(pairs):

@@ -11,6 +11,7 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -21,6 +22,16 @@ static int nthreads(int t) {
 #else
     (void)t;
     return 1;
+#endif
+}
+
+/* Wall-clock seconds (process CPU time in a build without OpenMP, where
+ * it is the same thing). */
+static double wall(void) {
+#ifdef _OPENMP
+    return omp_get_wtime();
+#else
+    return (double)clock() / CLOCKS_PER_SEC;
 #endif
 }
 
@@ -168,7 +179,8 @@ static void pv_push(pvec* v, uint64_t x) {
  * radixsort.cu), then scan forward while lo_j <= hi_i
  * (SapKernel.cu:1880-1913: break once d_pos[cur] > d_pos[i] + 2r). */
 static void sweep_group(int mode, const float* mn, const float* mx, int ax,
-                        uint32_t* ids, uint32_t m, pvec* out, int nt, uint32_t stride) {
+                        uint32_t* ids, uint32_t m, pvec* out, int nt, uint32_t parts,
+                        uint32_t part, double* t_sweep) {
     if (m < 2) return;
     uint32_t* keys = (uint32_t*)malloc((size_t)m * 4);
     float* lo = (float*)malloc((size_t)m * 4);
@@ -199,11 +211,16 @@ static void sweep_group(int mode, const float* mn, const float* mx, int ax,
             hi[k] = c + r;
         }
     }
+    /* sweep starts: slice `part` of `parts` equal slices of the sorted
+     * order (the whole order when parts == 1) */
+    const int64_t a0 = (int64_t)((uint64_t)m * part / parts);
+    const int64_t a1 = (int64_t)((uint64_t)m * (part + 1) / parts);
+    double t0 = wall();
 #pragma omp parallel num_threads(nt)
     {
         pvec local = {0, 0, 0};
 #pragma omp for schedule(dynamic, 64)
-        for (int64_t a = 0; a < (int64_t)m; a += stride) {
+        for (int64_t a = a0; a < a1; ++a) {
             uint32_t i = ids[a];
             float h = hi[a];
             for (uint32_t b = (uint32_t)a + 1; b < m && lo[b] <= h; ++b) {
@@ -221,6 +238,7 @@ static void sweep_group(int mode, const float* mn, const float* mx, int ax,
         }
         free(local.p);
     }
+    *t_sweep += wall() - t0;
     free(keys);
     free(lo);
     free(hi);
@@ -228,13 +246,16 @@ static void sweep_group(int mode, const float* mn, const float* mx, int ax,
 
 int64_t orc_sap_ref(int mode, const float* mn, const float* mx, uint32_t n,
                     uint32_t* pairs, int64_t cap, int threads) {
-    return orc_sap_ref_sampled(mode, mn, mx, n, 1, pairs, cap, threads);
+    return orc_sap_ref_sampled(mode, mn, mx, n, 1, 0, pairs, cap, threads, NULL);
 }
 
-int64_t orc_sap_ref_sampled(int mode, const float* mn, const float* mx, uint32_t n, uint32_t stride,
-                            uint32_t* pairs, int64_t cap, int threads) {
+int64_t orc_sap_ref_sampled(int mode, const float* mn, const float* mx, uint32_t n, uint32_t parts,
+                            uint32_t part, uint32_t* pairs, int64_t cap, int threads, double* secs) {
+    double t_start = wall(), t_var = 0.0;
+    if (secs) secs[0] = secs[1] = 0.0;
     if (n < 2) return 0;
-    if (stride == 0) stride = 1;
+    if (parts == 0) parts = 1;
+    part %= parts;
     int nt = nthreads(threads);
     /* centres: sphere xyz, or AABB midpoints */
     double mean[3] = {0, 0, 0}, var[3] = {0, 0, 0};
@@ -271,7 +292,7 @@ int64_t orc_sap_ref_sampled(int mode, const float* mn, const float* mx, uint32_t
         grp[q][gn[q]++] = i;
     }
     pvec all = {0, 0, 0};
-    for (int q = 0; q < 4; ++q) sweep_group(mode, mn, mx, axis, grp[q], gn[q], &all, nt, stride);
+    for (int q = 0; q < 4; ++q) sweep_group(mode, mn, mx, axis, grp[q], gn[q], &all, nt, parts, part, &t_var);
 
     /* Cross pass (cullCrossSphereMultiple :557-635, cullRelevantSphereMultiple
      * :968-1059): maxR over objects straddling a plane, then every object
@@ -306,14 +327,15 @@ int64_t orc_sap_ref_sampled(int mode, const float* mn, const float* mx, uint32_t
         }
         if ((h1 >= -maxR && l1 <= maxR) || (h2 >= -maxR && l2 <= maxR)) grp[0][rn++] = i;
     }
-    if (rn > 0 && rn < n) sweep_group(mode, mn, mx, axis, grp[0], rn, &all, nt, stride);
+    if (rn > 0 && rn < n) sweep_group(mode, mn, mx, axis, grp[0], rn, &all, nt, parts, part, &t_var);
     else if (rn == n) { /* every object is relevant: the quadrant sweeps are
                            not enough, sweep them all together */
         for (uint32_t i = 0; i < n; ++i) grp[0][i] = i;
-        sweep_group(mode, mn, mx, axis, grp[0], n, &all, nt, stride);
+        sweep_group(mode, mn, mx, axis, grp[0], n, &all, nt, parts, part, &t_var);
     }
 
     /* Canonicalise: sort + unique (Sap.cpp:269-291, cullIndex :2249-2265). */
+    double t_canon = wall();
     int idbits = 1;
     while (idbits < 32 && ((uint64_t)1 << idbits) < n) ++idbits;
     radix_sort_u64(all.p, all.n, 32 + ((idbits + 7) / 8) * 8);
@@ -326,9 +348,14 @@ int64_t orc_sap_ref_sampled(int mode, const float* mn, const float* mx, uint32_t
         }
         ++u;
     }
+    t_var += wall() - t_canon;
     for (int q = 0; q < 4; ++q) free(grp[q]);
     free(cen);
     free(all.p);
+    if (secs) {
+        secs[1] = t_var;
+        secs[0] = wall() - t_start - t_var;
+    }
     return u;
 }
 

@@ -48,12 +48,18 @@ int64_t orc_bf_sphere(const float* spheres, uint32_t n,
 int64_t orc_sap_ref(int mode, const float* mn, const float* mx, uint32_t n,
                     uint32_t* pairs, int64_t cap, int threads);
 
-/* Same, with the sweep started only from every stride-th sorted object of
- * each group (axis choice, sorts, partition and canonicalisation stay
- * full-size): a bounded sample of the reference algorithm's work at the
- * full scene's density, for timing.  stride = 1 is orc_sap_ref. */
-int64_t orc_sap_ref_sampled(int mode, const float* mn, const float* mx, uint32_t n, uint32_t stride,
-                            uint32_t* pairs, int64_t cap, int threads);
+/* Same, with the sweeps started only from slice `part` of `parts` equal,
+ * contiguous slices of each group's sorted order (axis choice, partition
+ * and the group sorts stay full-size): a bounded sample of the reference
+ * algorithm's work at the full scene's density, for timing; the slices
+ * part = 0 .. parts-1 together do one full call's sweep work.  parts = 1
+ * is orc_sap_ref.  When secs is not NULL the call splits its wall time:
+ * secs[1] = the stages that scale with the number of sweep starts (the
+ * sweep loops and the sort + unique of the pairs they find), secs[0] =
+ * everything else (centres, axis choice, partition, group sorts).  Averaged
+ * over the parts, secs[0] + parts * secs[1] is one full call's time. */
+int64_t orc_sap_ref_sampled(int mode, const float* mn, const float* mx, uint32_t n, uint32_t parts,
+                            uint32_t part, uint32_t* pairs, int64_t cap, int threads, double* secs);
 
 /* The reference's output format (SapKernel.cu:2249-2360, Sap.cpp:326-329)
  * from a sorted unique (i<j) list: both directions (i,j) and (j,i) sorted by

@@ -43,6 +43,31 @@ def test_sap_restatement_equals_brute_force(oracle_lib, seed):
     assert np.array_equal(oracle_lib.sap_ref(1, sp), oracle_lib.bf_sphere(sp))
 
 
+def test_sap_slices_cover_the_full_sweep(oracle_lib):
+    """The timing sample of the CPU baseline: the sweeps started from slice
+    k of `parts` contiguous slices, over every k, find exactly the full
+    call's pairs, and each call reports non-negative stage times."""
+    import ctypes as C
+    rng = np.random.default_rng(5)
+    n = 6000
+    c = rng.normal(size=(n, 3)) * np.array([40.0, 9.0, 3.0])
+    h = np.exp(rng.normal(-1.0, 0.5, (n, 3))).clip(0.05, 2.0)
+    mn = np.concatenate([c - h, np.zeros((n, 1))], 1).astype(np.float32)
+    mx = np.concatenate([c + h, np.zeros((n, 1))], 1).astype(np.float32)
+    full = oracle_lib.sap_ref(0, mn, mx)
+    L = oracle_lib.lib()
+    got = set()
+    for k in range(8):
+        out = np.empty((len(full), 2), np.uint32)
+        secs = np.full(2, -1.0)
+        m = L.orc_sap_ref_sampled(0, mn.ctypes.data, mx.ctypes.data, C.c_uint32(n), C.c_uint32(8), C.c_uint32(k),
+                                  out.ctypes.data, C.c_int64(len(full)), 0, secs.ctypes.data)
+        assert 0 < m <= len(full) and (secs >= 0).all()
+        got |= {tuple(p) for p in out[:m]}
+        assert oracle_lib.sap_ref_sampled(0, mn, mx, 8, k)[0] == m
+    assert got == {tuple(p) for p in full}
+
+
 def test_rb_reference_step_matches_reference_kernels(oracle_lib):
     """The FP32 restatement reproduces the reference kernels bit for bit."""
     g = load("rb_ref_step_golden.npz")
