@@ -118,7 +118,7 @@ struct gsap_sap {
 
 static void free_scratch(gsap_sap* h) {
     BpScratch& s = h->s;
-    void* ptrs[] = {s.ctrl, s.scenes, s.scenes_next, s.partials, s.scene_done, s.work_start, s.objcell, s.objscene,
+    void* ptrs[] = {s.ctrl, s.scenes, s.scenes_next, s.partials, s.scene_done, s.work_start, s.objscene,
                     s.keys[0], s.keys[1], s.vals[0], s.vals[1], s.status, s.rowcnt, s.rowoff, s.tmp_pairs,
                     s.grp_pairs, s.tmp_rank, s.smin, s.smax, s.longrows, s.tile_sums};
     for (void* p : ptrs)
@@ -176,7 +176,6 @@ extern "C" gsap_sap* gsap_sap_create(uint32_t max_n, const gsap_config* cfg) {
     A((void**)&s.partials, sizeof(PcaPartial) * s.max_work);
     A((void**)&s.scene_done, 4ull * c.max_scenes);
     A((void**)&s.work_start, 4ull * (c.max_scenes + 1));
-    A((void**)&s.objcell, 4ull * max_n);
     if (c.max_scenes > 1) A((void**)&s.objscene, 4ull * max_n);
     for (int k = 0; k < 2; ++k) {
         A((void**)&s.keys[k], 4ull * ecap);
@@ -302,8 +301,7 @@ static gsap_status record(gsap_sap* h, const Call& c, cudaStream_t st, bool time
     mark();
     const uint32_t* count = &s.ctrl->entry_count;
     int src = 0;
-    SortGather gather{c.mn, c.mode == GSAP_MODE_AABB ? c.mx : nullptr, s.objcell, s.objscene, s.scenes,
-                      s.smin, s.smax};
+    SortGather gather{c.mn, c.mode == GSAP_MODE_AABB ? c.mx : nullptr, s.smin, s.smax};
     for (int p = 0; p < passes; ++p) {
         // the last pass's object ids go into the sweep records, not into a value array
         const bool last = p == passes - 1;

@@ -84,6 +84,12 @@ struct PcaPartial {
 };
 
 // Device scratch of a broadphase handle.
+// A sweep entry's value: its object index in the low bits and its owner
+// flags on top (bit 30: the entry's cell is the object's lowest on u2, bit
+// 31: on u3).  The entry capacity is below 2^30, so object indices fit.
+constexpr uint32_t kFlagShift = 30;
+constexpr uint32_t kObjMask = (1u << kFlagShift) - 1u;
+
 struct BpScratch {
     Ctrl* ctrl;
     Scene* scenes;
@@ -91,10 +97,9 @@ struct BpScratch {
     uint32_t* scene_done;      // per-scene PCA completion counters
     Scene* scenes_next;        // temporal mode: per-scene parameters for the next call
     uint32_t* work_start;      // per-scene first work item (S+1), batched plan
-    uint32_t* objcell;         // per object: (c2lo << 16) | c3lo
     uint32_t* objscene;        // per object scene id (batched only)
     uint32_t* keys[2];
-    uint32_t* vals[2];
+    uint32_t* vals[2];         // object index | owner flags << kFlagShift
     uint64_t* status;          // look-back words (per tile and digit)
     // Sweep entries in sorted order, one 32-byte record each.  Boxes:
     // smin = (lo.xyz, object index bits), smax = (hi.xyz, owner flag bits).
@@ -149,9 +154,6 @@ cudaError_t launch_project(const BpScratch& s, const BpArgs& a, int passes, cuda
 struct SortGather {
     const float4* mn;
     const float4* mx;          // nullptr in sphere mode
-    const uint32_t* objcell;
-    const uint32_t* objscene;  // nullptr for one scene
-    const Scene* scenes;
     float4* smin;
     float4* smax;
 };

@@ -112,7 +112,6 @@ __global__ void __launch_bounds__(kThreads) k_project(BpScratch S, BpArgs A) {
                 clo[k] = (c2a << 16) | c3a;
                 ncl[k] = (n2 << 16) | n3;
                 r = n2 * n3;
-                S.objcell[i] = clo[k];
                 if (S.objscene) S.objscene[i] = scene;
             } else {
                 bad = true;
@@ -149,8 +148,10 @@ __global__ void __launch_bounds__(kThreads) k_project(BpScratch S, BpArgs A) {
             for (uint32_t x3 = 0; x3 < n3; ++x3, ++pos) {
                 uint32_t key = ((bb + (c2a + x2) * G3 + (c3a + x3)) << Q) | qlo[k];
                 if (pos < S.entry_cap) {  // entries past the capacity are counted, never stored
+                    // owner flags: is this the object's lowest cell on u2 / u3?
+                    const uint32_t fl = (x2 == 0 ? 1u : 0u) | (x3 == 0 ? 2u : 0u);
                     S.keys[0][pos] = key;
-                    S.vals[0][pos] = i;
+                    S.vals[0][pos] = i | (fl << kFlagShift);
                     atomicAdd(&s_hist[0][key & 255u], 1u);  // later digits: counted by the sort passes
                 }
             }

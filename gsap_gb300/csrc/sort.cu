@@ -59,7 +59,6 @@ __global__ void __launch_bounds__(kThreads, 2) k_onesweep(BpScratch S, const uin
     const uint32_t ntiles = (n + TILE - 1) / TILE;
     const int shift = 8 * pass;
     const uint32_t tag = (S.ctrl->epoch << 3) | (uint32_t)pass;
-    const uint32_t gq = G.smin ? S.ctrl->qbits : 0u;  // key = (bucket << Q) | q
     const uint32_t lt = lanemask_lt();
 
     s_gdig[tid] = cta_excl_scan256(S.ctrl->hist[pass][tid], s_scan);
@@ -163,22 +162,19 @@ __global__ void __launch_bounds__(kThreads, 2) k_onesweep(BpScratch S, const uin
             kout[g] = kk;
             if (vout) vout[g] = vv;
             if (G.smin) {  // last pass of the broadphase: entries in sorted order
-                // owner flags: is this entry's cell the object's lowest
-                // column (u2) / row (u3)?  A pair is owned by the cell of
-                // (max lo2, max lo3), which both objects touch, so the cell
-                // owns it iff each coordinate is some member's lowest.
-                const Scene* sc = G.scenes + (G.objscene ? __ldg(G.objscene + vv) : 0u);
-                const uint32_t b = (kk >> gq) - __ldg(&sc->bucket_base), g3 = __ldg(&sc->G3);
-                const uint32_t b2 = b / g3, b3 = b - b2 * g3, oc = __ldg(G.objcell + vv);
-                const uint32_t fl = (b2 == (oc >> 16) ? 1u : 0u) | (b3 == (oc & 0xFFFFu) ? 2u : 0u);
-                const float4 lo = __ldg(G.mn + vv);
+                // The value holds the object index and the entry's owner
+                // flags (set by the projection): a pair is owned by the cell
+                // of (max lo2, max lo3), which both objects touch, so the
+                // cell owns it iff each coordinate is some member's lowest.
+                const uint32_t obj = vv & kObjMask, fl = vv >> kFlagShift;
+                const float4 lo = __ldg(G.mn + obj);
                 if (G.mx) {  // boxes: index and flags ride in the unused w lanes
-                    const float4 hi = __ldg(G.mx + vv);
-                    G.smin[g] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(vv));
+                    const float4 hi = __ldg(G.mx + obj);
+                    G.smin[g] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(obj));
                     G.smax[g] = make_float4(hi.x, hi.y, hi.z, __uint_as_float(fl));
                 } else {     // spheres: radius in w, index and flags in the second record
                     G.smin[g] = lo;
-                    G.smax[g] = make_float4(__uint_as_float(vv), __uint_as_float(fl), 0.f, 0.f);
+                    G.smax[g] = make_float4(__uint_as_float(obj), __uint_as_float(fl), 0.f, 0.f);
                 }
             }
         }
@@ -238,7 +234,7 @@ cudaError_t launch_sort_pass(const BpScratch& s, int pass, int passes, const uin
                              uint32_t spin, cudaStream_t st, const SortGather* gather, bool count_next) {
     SortGather G;
     if (gather) G = *gather;
-    else G = SortGather{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    else G = SortGather{nullptr, nullptr, nullptr, nullptr};
     static int grid = 0;
     if (grid == 0) {
         int per_sm = 0;
