@@ -171,6 +171,29 @@ __global__ void __launch_bounds__(kThreads) k_pca(BpScratch S, BpArgs A) {
 // the next call's parameters instead and leaves the counters to the main
 // branch.  A separate launch keeps the FP64 tail's registers out of the
 // streaming kernel.
+// Quantisation bits of the key's low field when `total` buckets take the
+// high bits of a key_bits-bit key (0: the grid does not fit).
+__device__ __forceinline__ uint32_t key_q_bits(uint32_t key_bits, uint32_t total) {
+    uint32_t bbits = 0;
+    while (bbits < 32 && (1ull << bbits) < (uint64_t)total) ++bbits;
+    uint32_t q = key_bits > bbits ? key_bits - bbits : 0u;
+    return q > 24 ? 24u : q;
+}
+
+// The per-call pipeline counters back to zero (the epoch is advanced by the
+// caller).
+__device__ __forceinline__ void reset_counters(Ctrl* C) {
+    C->entry_count = 0;
+    C->pair_count = 0ull;
+    for (int p = 0; p < kMaxPasses + 4; ++p) C->tile_ctr[p] = 0;
+    C->sweep_ctr = 0;
+    C->scan_ctr = 0;
+    C->scan_total = 0;
+    C->long_rows = 0;
+    C->tests = 0ull;
+    C->iters = 0ull;
+}
+
 __global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, uint64_t entry_cap, int temporal) {
     Scene* const out = temporal ? S.scenes_next : S.scenes;
     __shared__ uint32_t s_flag;
@@ -183,6 +206,15 @@ __global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, 
     // partials that k_pca wrote are read)
     const uint32_t nw0 = A.scene_off ? S.work_start[scene + 1] - wfirst : work_items(A.n);
     const uint32_t nw = wfirst < A.num_work ? min(nw0, A.num_work - wfirst) : 0u;
+    // Thread 0's loads for later (the pilot object, and the epoch that the
+    // one-scene reset below advances) are in flight during the merge.
+    const bool one = A.num_scenes == 1;
+    float px = 0.f, py = 0.f, pz = 0.f;
+    uint32_t epoch0 = 0;
+    if (tid == 0) {
+        pilot_of(A, sb, se, px, py, pz);
+        if (one && !temporal) epoch0 = S.ctrl->epoch;
+    }
     // Combine the scene's partials in float-float (two-sum) arithmetic on the
     // FP32 pipes: thread t merges items t, t+256, ..., then warps and the CTA
     // merge in a fixed order (deterministic); only the final hi + lo pairs go
@@ -231,20 +263,43 @@ __global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, 
         const double* t = s_tot;
         for (int k = 0; k < 3; ++k) { z.sd[k] = t[k]; z.sh[k] = t[9 + k]; z.hmax[k] = t[kPcaQ + k]; }
         for (int k = 0; k < 6; ++k) { z.sdd[k] = t[3 + k]; z.shh[k] = t[12 + k]; }
-        float px = 0.f, py = 0.f, pz = 0.f;
-        pilot_of(A, sb, se, px, py, pz);
         z.pilot[0] = px; z.pilot[1] = py; z.pilot[2] = pz;
         z.n = (double)(se - sb);
         Scene sc;
         choose_scene(z, A, entry_cap, A.n, sc);
-        out[scene] = sc;
-        if (A.num_scenes == 1) {
-            s_flag = 1u;  // the only scene: this CTA is the last one
+        if (one) {
+            // The only scene: its bucket base is 0, the key layout follows
+            // from its own grid, and the record is stored once, complete
+            // (the general tail below reads the records back from memory).
+            const uint32_t total = sc.G2 * sc.G3;
+            const uint32_t q = key_q_bits(A.key_bits, total);
+            if (q == 0) atomicOr(&C->error, kErrCellRange);
+            sc.bucket_base = 0;
+            sc.q_scale = __fdiv_rn((float)(1u << q), sc.q_range);
+            out[0] = sc;
+            C->scenes_done = 0;
+            if (temporal) {
+                C->qbits_next = q;
+                C->key_bits_next = A.key_bits;
+                C->total_buckets_next = total;
+            } else {
+                C->qbits = q;
+                C->key_bits = A.key_bits;
+                C->total_buckets = total;
+                reset_counters(C);
+                C->epoch = epoch0 + 1u;
+            }
         } else {
+            out[scene] = sc;
             __threadfence();
             uint32_t old = atomicAdd(&C->scenes_done, 1u);
             s_flag = (old == A.num_scenes - 1) ? 1u : 0u;
         }
+    }
+    if (one) {
+        if (!temporal)
+            for (int p = 0; p < kMaxPasses; ++p) C->hist[p][tid] = 0u;
+        return;
     }
     __syncthreads();
     if (!s_flag) return;
@@ -276,10 +331,7 @@ __global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, 
     __shared__ uint32_t s_q;
     if (tid == 0) {
         uint32_t total = s_carry;
-        uint32_t bbits = 0;
-        while (bbits < 32 && (1ull << bbits) < (uint64_t)total) ++bbits;
-        uint32_t q = A.key_bits > bbits ? A.key_bits - bbits : 0u;
-        if (q > 24) q = 24;
+        const uint32_t q = key_q_bits(A.key_bits, total);
         if (q == 0) atomicOr(&C->error, kErrCellRange);
         s_q = q;
         C->scenes_done = 0;
@@ -299,15 +351,7 @@ __global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, 
         C->qbits = s_q;
         C->key_bits = A.key_bits;
         C->total_buckets = s_carry;
-        C->entry_count = 0;
-        C->pair_count = 0ull;
-        for (int p = 0; p < kMaxPasses + 4; ++p) C->tile_ctr[p] = 0;
-        C->sweep_ctr = 0;
-        C->scan_ctr = 0;
-        C->scan_total = 0;
-        C->long_rows = 0;
-        C->tests = 0ull;
-        C->iters = 0ull;
+        reset_counters(C);
         C->epoch = C->epoch + 1u;
     }
     for (int p = 0; p < kMaxPasses; ++p) C->hist[p][tid] = 0u;
@@ -334,15 +378,7 @@ __global__ void k_reset(BpScratch S) {
     Ctrl* C = S.ctrl;
     const uint32_t tid = threadIdx.x;
     if (tid == 0) {
-        C->entry_count = 0;
-        C->pair_count = 0ull;
-        for (int p = 0; p < kMaxPasses + 4; ++p) C->tile_ctr[p] = 0;
-        C->sweep_ctr = 0;
-        C->scan_ctr = 0;
-        C->scan_total = 0;
-        C->long_rows = 0;
-        C->tests = 0ull;
-        C->iters = 0ull;
+        reset_counters(C);
         C->epoch = C->epoch + 1u;
     }
     for (int p = 0; p < kMaxPasses; ++p) C->hist[p][tid] = 0u;
