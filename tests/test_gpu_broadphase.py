@@ -270,6 +270,42 @@ def test_temporal_mode_is_exact_frame_to_frame(cuda, oracle_lib, graph):
     frame(scenes.jitter(c2, seed=7), h2)
 
 
+@pytest.mark.parametrize("batched", [False, True])
+def test_temporal_next_grid_is_the_inputs_pca(cuda, batched):
+    """In temporal mode the projection takes the call's PCA sums (one
+    partial per projection CTA) and the scene solve prepares the next call's
+    grid from them: after a temporal call on frame B the handle's axes,
+    eigenvalues and mean are those a plain call computes on B (the two sum
+    the same terms in a different order)."""
+    import torch
+    from gsap_gb300 import Sap, scenes
+    n = 50_000
+    c, h, _ = scenes.aabb_gauss_parts(n, seed=41, std=(30.0, 9.0, 3.0))
+    mn = np.concatenate([c - h, np.zeros((n, 1), np.float32)], 1)
+    mx = np.concatenate([c + h, np.zeros((n, 1), np.float32)], 1)
+    b = scenes.jitter(c, seed=5) + np.float32([4.0, -2.0, 1.0])
+    mnb = np.concatenate([b - h, np.zeros((n, 1), np.float32)], 1)
+    mxb = np.concatenate([b + h, np.zeros((n, 1), np.float32)], 1)
+    off = torch.tensor([0, n // 3, n], dtype=torch.int32, device=cuda)
+    S = 2 if batched else 1
+
+    def call(sap, a, z, temporal):
+        if batched:
+            sap.broadphase_batched(to_dev(a, cuda), to_dev(z, cuda), off, temporal=temporal)
+        else:
+            sap.broadphase(to_dev(a, cuda), to_dev(z, cuda), sorted=True, temporal=temporal)
+
+    tsap, psap = Sap(n, max_scenes=S), Sap(n, max_scenes=S)
+    call(tsap, mn, mx, True)    # no previous grid: plain pipeline
+    call(tsap, mnb, mxb, True)  # temporal: sweeps with A's grid, prepares B's
+    call(psap, mnb, mxb, False)
+    for s in range(S):
+        t, p = tsap.scene_axes(s), psap.scene_axes(s)
+        assert np.allclose(t["axes"], p["axes"], rtol=0, atol=1e-9)
+        assert np.allclose(t["eig"], p["eig"], rtol=1e-9, atol=0)
+        assert np.allclose(t["mean"], p["mean"], rtol=1e-12, atol=1e-9)
+
+
 def test_batched_temporal_frames_are_exact(cuda, oracle_lib):
     """GSAP_FLAG_TEMPORAL on batched calls: each scene's pairs stay the brute
     force's from frame to frame, including a frame where scene sizes change
