@@ -158,6 +158,43 @@ def test_gauss_1m_against_cpu_sap(cuda, oracle_lib, axis_mode):
         assert abs(abs(ax @ R[:, 0]) - 1.0) < 1e-3
 
 
+def test_large_scene_sampled_rows_against_brute_force(cuda):
+    """16,777,216 boxes (the 1M workload's object density at 16 times the
+    objects; about 95M pairs): every reported pair overlaps, the list is
+    sorted and unique, and for 512 sampled objects the partners in the list
+    are exactly those a brute-force test against all boxes finds (run on the
+    GPU with torch as the checker; the CPU oracle is too slow at this size)."""
+    import torch
+    from gsap_gb300 import Sap, scenes
+    n = 1 << 24
+    f = 16.0 ** (1.0 / 3.0)
+    c, h, _ = scenes.aabb_gauss_parts(n, seed=77, std=(100.0 * f, 20.0 * f, 5.0 * f))
+    mn = torch.from_numpy(np.concatenate([c - h, np.zeros((n, 1), np.float32)], 1)).to(cuda)
+    mx = torch.from_numpy(np.concatenate([c + h, np.zeros((n, 1), np.float32)], 1)).to(cuda)
+    del c, h
+    sap = Sap(n)
+    p = sap.broadphase(mn, mx, sorted=True).long()
+    sap.close()
+    P = p.shape[0]
+    assert P > 2 * n
+    a, b = p[:, 0], p[:, 1]
+    assert bool((a < b).all())
+    key = a * n + b
+    assert bool((key[1:] > key[:-1]).all())
+    del key
+    step = 1 << 24
+    for s in range(0, P, step):
+        i, j = a[s:s + step], b[s:s + step]
+        assert bool(((mn[i, :3] <= mx[j, :3]) & (mn[j, :3] <= mx[i, :3])).all())
+    g = torch.Generator().manual_seed(3)
+    for s in torch.randint(0, n, (512,), generator=g).tolist():
+        hit = ((mn[s, :3] <= mx[:, :3]) & (mn[:, :3] <= mx[s, :3])).all(1)
+        hit[s] = False
+        want = torch.nonzero(hit).flatten()
+        got = torch.cat([b[a == s], a[b == s]]).sort().values
+        assert torch.equal(got, want), s
+
+
 def test_autotune_keeps_the_pair_set(cuda, oracle_lib):
     """Every setting of the tuning grid gives the same pair set; the tuner's
     choice lies in the grid and the handle keeps using it."""
