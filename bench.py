@@ -424,6 +424,32 @@ def run_extras(args, dev, stream):
                                              and int(scnt.item()) == len(bf))
     out["small_16k"] = small
     del ssap, spairs
+    # --- large case: 16,777,216 AABBs at the 1M workload's object density
+    # (spread scaled by 16^(1/3)); one input set of 512 MiB, larger than L2
+    nl = 1 << 24
+    (lmn, lmx), = make_inputs(0, nl, 1)[0]
+    dlmn, dlmx = torch.from_numpy(lmn).to(dev), torch.from_numpy(lmx).to(dev)
+    del lmn, lmx
+    lsap = Sap(nl)
+    lcfg = lsap.autotune(dlmn, dlmx, reps=3)
+    lpairs = torch.empty((8 * nl, 2), dtype=torch.int32, device=dev)
+    lcnt = torch.zeros(1, dtype=torch.int64, device=dev)
+    for _ in range(3):
+        lsap.broadphase_async(dlmn, dlmx, lpairs, lcnt, sorted=True, graph=True, stream=stream)
+    torch.cuda.synchronize()
+    lsap.check()
+    e0.record(stream)
+    for _ in range(10):
+        lsap.broadphase_async(dlmn, dlmx, lpairs, lcnt, sorted=True, graph=True, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    lsap.check()
+    l_ms = e0.elapsed_time(e1) / 10
+    out["large_16m"] = {"n": nl, "pairs": int(lcnt.item()), "ms_per_call": round(l_ms, 4),
+                        "mobjects_per_s": round(nl / (l_ms / 1e3) / 1e6, 1), "settings": lcfg,
+                        "sample": "one seeded 16,777,216-AABB scene, 10 graph calls after the autotuner"}
+    lsap.close()
+    del lsap, lpairs, dlmn, dlmx
     # --- batched broadphase: 4096 scenes, sizes log-uniform in [64, 65536]
     S = args.scenes
     mn, mx, off = scenes.batched_aabb(S=S, seed=7)
