@@ -71,6 +71,19 @@ def traffic_table():
     return out
 
 
+def profile_metric(kernel: str, name: str):
+    """A percentage from a committed ncu summary (profiles/<kernel>_gauss1m.md
+    table row `| name | value % |`), as a fraction, or None."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_gauss1m.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        cells = [c.strip() for c in line.strip().strip("|").split("|")]
+        if len(cells) == 2 and cells[0] == name and cells[1].endswith("%"):
+            return round(float(cells[1].rstrip("%").strip()) / 100.0, 4)
+    return None
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons during the timed region."""
 
@@ -363,7 +376,11 @@ def run_ours(args, world, rank, local):
                    {"sort_bits": args.sort_bits or 32, "cell_factor": args.cell_factor or 2.0, "autotuned": False}},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": f"stage:{dom}",
-                     "peak_kind": peak_kind},
+                     "peak_kind": peak_kind,
+                     # what limits it instead: the L1 data path (one ncu --set full capture)
+                     "limiter": {"l1tex_throughput_frac": profile_metric(f"k_{dom}", "L1/TEX Cache Throughput"),
+                                 "dram_throughput_frac": profile_metric(f"k_{dom}", "DRAM Throughput"),
+                                 "source": f"profiles/k_{dom}_gauss1m.md"}},
         "pipeline_roofline": {"bytes_alg": alg["total"], "achieved_gbs": round(pipe_gbs, 1),
                               "frac": round(pipe_gbs / peak, 4), "formula": "156 n + 8 P"},
         "stage_ms": {k: round(v, 4) for k, v in st_ms.items()},
