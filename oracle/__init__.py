@@ -14,7 +14,9 @@ host and is used to pin the restatement and to generate ``tests/golden``.
 from __future__ import annotations
 
 import ctypes as C
+import fcntl
 import os
+import platform
 import subprocess
 
 import numpy as np
@@ -25,17 +27,37 @@ _REF = None
 
 
 _BUILT = False
+_STAMP = os.path.join(HERE, ".built-for")  # machine type liboracle.so was built for
+
+
+def _up_to_date() -> bool:
+    lib = os.path.join(HERE, "liboracle.so")
+    if not (os.path.exists(lib) and os.path.exists(_STAMP)):
+        return False
+    with open(_STAMP) as fh:
+        if fh.read() != platform.machine():
+            return False
+    srcs = [os.path.join(HERE, f) for f in ("bp.c", "rb.c", "oracle.h", "Makefile")]
+    return os.path.getmtime(lib) >= max(os.path.getmtime(f) for f in srcs)
 
 
 def build(ref: bool = False) -> None:
-    """Compile liboracle.so (always from source: a library built on another
-    machine type is never reused) and the reference harness when ``ref``."""
+    """Compile liboracle.so from source unless this machine type already
+    built it from the current sources (a library built on another machine
+    type is never reused), and the reference harness when ``ref``.  Builds
+    are serialised across processes by a lock file, so workers that start
+    together never load a library another one is still writing."""
     global _BUILT
-    if not _BUILT:
-        subprocess.run(["make", "-s", "-B", "-C", HERE, "liboracle.so"], check=True)
-        _BUILT = True
-    if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    with open(os.path.join(HERE, ".build.lock"), "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        if not _BUILT:
+            if not _up_to_date():
+                subprocess.run(["make", "-s", "-B", "-C", HERE, "liboracle.so"], check=True)
+                with open(_STAMP, "w") as fh:
+                    fh.write(platform.machine())
+            _BUILT = True
+        if ref:
+            subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
 
 
 def _i64(x):

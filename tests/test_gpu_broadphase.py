@@ -412,6 +412,15 @@ def test_degenerate_and_far_from_origin_scenes(cuda, oracle_lib):
     mn = np.concatenate([c - h, np.zeros((4000, 1), np.float32)], 1)
     mx = np.concatenate([c + h, np.zeros((4000, 1), np.float32)], 1)
     assert np.array_equal(run_bp(sap, mn, mx, cuda), oracle_lib.bf_aabb(mn, mx))
+    # a box overlapping 3000 others: its row is longer than a warp sorts in
+    # shared memory (rank placement path)
+    big = np.concatenate([np.float32([[15.0, 15.0, 7.0]]), c[:2999]], 0)
+    hb = np.concatenate([np.float32([[40.0, 40.0, 40.0]]), h[:2999]], 0)
+    mn = np.concatenate([big - hb, np.zeros((3000, 1), np.float32)], 1)
+    mx = np.concatenate([big + hb, np.zeros((3000, 1), np.float32)], 1)
+    got = run_bp(sap, mn, mx, cuda)
+    assert np.count_nonzero(got[:, 0] == 0) == 2999
+    assert np.array_equal(got, oracle_lib.bf_aabb(mn, mx))
     far = (rng.uniform(0, 40, (4000, 3)) + 1.0e6).astype(np.float32)
     mn = np.concatenate([far - h, np.zeros((4000, 1), np.float32)], 1)
     mx = np.concatenate([far + h, np.zeros((4000, 1), np.float32)], 1)

@@ -102,6 +102,32 @@ def test_collision_matches_reference_format(cuda, oracle_lib):
         assert np.array_equal(ent[:n_ent].cpu().numpy(), want_ent)
 
 
+def test_collision_format_with_long_rows(cuda, oracle_lib):
+    """Both-direction format where rows are longer than the row buckets:
+    a clump of 150 coincident spheres (rows of 149 entries each way) and a
+    large sphere overlapping 1500 small ones (a row past the warp-sort
+    limit), beside a scattered background."""
+    import torch
+    from gsap_gb300 import MODE_SPHERE, Sap
+    rng = np.random.default_rng(23)
+    bg = rng.uniform(-40, 40, (3000, 3)).astype(np.float32)
+    clump = np.tile(np.float32([[30.0, 30.0, 30.0]]), (150, 1))
+    ring = rng.uniform(-3, 3, (1500, 3)).astype(np.float32)
+    c = np.concatenate([ring[:1], bg, clump, ring], 0)
+    r = np.full((len(c), 1), 0.25, np.float32)
+    r[0] = 6.0  # the large sphere, id 0
+    s = np.concatenate([c, r], 1)
+    n = len(s)
+    sap = Sap(n, mode=MODE_SPHERE, pair_factor=64)
+    pairs = torch.empty((64 * n, 2), dtype=torch.int32, device=cuda)
+    ent = torch.empty(n + 1, dtype=torch.int32, device=cuda)
+    n_pairs, n_ent = sap.collision(0.0, torch.from_numpy(s).to(cuda), pairs, ent)
+    want_pairs, want_ent = oracle_lib.both_directions(oracle_lib.bf_sphere(s))
+    assert n_pairs == len(want_pairs) and n_ent == len(want_ent)
+    assert np.array_equal(pairs[:n_pairs].cpu().numpy(), want_pairs)
+    assert np.array_equal(ent[:n_ent].cpu().numpy(), want_ent)
+
+
 def config_params():
     return dict(dt=1.0 / 600.0, k=2e4, eta=50.0, kt=0.1, gravity_y=-9.81, box_lo=(0.0, 0.0, 0.0),
                 box_hi=(200.0, 200.0, 200.0))

@@ -67,6 +67,7 @@ def test_two_rank_scene_shards_match_single_process():
 
     import oracle
     from gsap_gb300 import scenes
+    oracle.build()  # once, before the workers load it
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
