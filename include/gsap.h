@@ -118,7 +118,7 @@ gsap_status gsap_sap_collision(gsap_sap* h, float spacing, const float* d_sphere
                                int32_t* h_num_pairs, int32_t* h_num_entries,
                                uint64_t pair_cap, uint64_t entry_cap, void* stream);
 
-/* North-star form of the per-step broadphase (same pipeline as
+/* AABB-list form of the per-step broadphase (same pipeline as
  * Sap::collision, AABB or sphere predicate from cfg.mode).
  * d_min / d_max: n float4 each (xyz used; for GSAP_MODE_SPHERE d_min holds
  * the spheres and d_max may be NULL).  Writes up to pair_cap pairs (i, j),

@@ -15,7 +15,7 @@ from conftest import GOLDEN
 
 pytestmark = pytest.mark.gpu
 
-REL_TOL = 1e-5  # spec bound for one step vs the reference FP32 step
+REL_TOL = 1e-5  # bound for one step against the reference FP32 step
 
 
 def relerr(a, b):
