@@ -18,6 +18,10 @@ and writes:
                          and its state after each of 3 reference steps
   demo_2_1024.npz        the per-frame pair dumps of cudaPhysics/2_1024.txt
                          (CPU brute-force pairs of the demo with both spheres)
+  rb_demo_steps_golden.npz
+                         the headless demo's scene (hexagon bodies of two
+                         sizes, 256 bodies packed into contact) and its state
+                         after each of 4 reference steps
 """
 from __future__ import annotations
 
@@ -178,24 +182,45 @@ def ref_step(R, s, dt, spM, dpM, max_vel):
     return len(both), len(ent)
 
 
-def make_rb(rng, out):
+def run_rb(s, dt, spM, dpM, max_vel, steps, out):
+    """The scene's initial state and its state after each reference step."""
     R = oracle.ref_lib()
     for name in ("ref_normalize_quats", "ref_integrate", "ref_update_particle_data", "ref_prepare", "ref_clear_force", "ref_pair_force",
                  "ref_update_velocity"):
         getattr(R, name).restype = None
-    s = rb_scene(rng)
-    dt, spM, dpM, max_vel = 0.025, 2.1, 0.8, 0.25 / 0.01
     data = {f"init__{k}": v.copy() for k, v in s.items()}  # quaternions as uploaded (raw)
-    R.ref_normalize_quats.restype = None
     R.ref_normalize_quats(s["quat"].ctypes.data_as(C.c_void_p), len(s["quat"]))  # setRbData
-    for step in range(3):
+    for step in range(steps):
         npairs, nent = ref_step(R, s, dt, spM, dpM, max_vel)
         for k in ("pos", "quat", "lin_vel", "ang_vel", "p_pos", "p_vel", "p_force", "inv_inertia"):
             data[f"step{step}__{k}"] = s[k].copy()
         data[f"step{step}__npairs"] = np.int64(npairs)
         print(f"  rb step {step}: both-direction pairs={npairs} entries={nent}")
     data["params"] = np.array([dt, spM, dpM, max_vel, -5.0], np.float32)
+    data["steps"] = np.int64(steps)
     np.savez_compressed(out, **data)
+
+
+def make_rb(rng, out):
+    run_rb(rb_scene(rng), 0.025, 2.1, 0.8, 0.25 / 0.01, 3, out)
+
+
+def make_rb_demo(out):
+    """The headless demo's scene (DemoParticles::init layout: hexagon bodies
+    of two sizes, random orientations and spins, gsap_gb300/demo.py) with
+    256 bodies packed to 0.3 of the demo's spacing so they touch from the
+    first step, under the demo's step parameters, for 4 reference steps."""
+    from gsap_gb300 import demo
+    sc = demo.demo_scene(256, n_row=8, seed=7)
+    keys = ("pos", "quat", "lin_vel", "ang_vel", "shape_idx", "p_start", "n_part", "inv_mass", "inv_inertia",
+            "ref_pos", "ref_mass", "shape_inv_inertia")
+    s = {k: np.ascontiguousarray(sc[k]).copy() for k in keys}
+    s["pos"][:, :3] *= np.float32(0.3)
+    npart = int(sc["n_particles"])
+    for k in ("p_pos", "p_vel", "p_force"):
+        s[k] = np.zeros((npart, 4), np.float32)
+    s["p_mass"] = np.zeros(npart, np.float32)
+    run_rb(s, demo.DT, demo.SP_MULTIP, demo.DP_MULTIP, demo.SMALL_RADIUS / demo.VCAP_DT, 4, out)
 
 
 # ---------------------------------------------------------- 2_1024.txt dump
@@ -237,13 +262,23 @@ def make_demo_dump(ref, out):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=DEFAULT_REF)
+    ap.add_argument("--only", default=None, choices=["aabb", "rb", "dump", "rb_demo"],
+                    help="write one fixture (default: all)")
     a = ap.parse_args()
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "liboracle.so", "ref", f"REF={a.ref}"],
                    check=True)
     rng = np.random.default_rng(20240917)
-    make_aabb(rng, os.path.join(HERE, "aabb_bf_golden.npz"))
-    make_rb(rng, os.path.join(HERE, "rb_ref_step_golden.npz"))
-    make_demo_dump(a.ref, os.path.join(HERE, "demo_2_1024.npz"))
+    aabb_out = os.path.join(HERE, "aabb_bf_golden.npz")
+    if a.only in (None, "aabb"):
+        make_aabb(rng, aabb_out)
+    else:
+        aabb_cases(rng)  # advances the generator as make_aabb does, for the fixtures after it
+    if a.only in (None, "rb"):
+        make_rb(rng, os.path.join(HERE, "rb_ref_step_golden.npz"))
+    if a.only in (None, "dump"):
+        make_demo_dump(a.ref, os.path.join(HERE, "demo_2_1024.npz"))
+    if a.only in (None, "rb_demo"):
+        make_rb_demo(os.path.join(HERE, "rb_demo_steps_golden.npz"))
 
 
 if __name__ == "__main__":

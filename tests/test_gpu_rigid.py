@@ -23,8 +23,12 @@ def relerr(a, b):
     return np.abs(a - b).max() / max(np.abs(b).max(), 1e-30)
 
 
-def golden_rb():
-    return np.load(os.path.join(GOLDEN, "rb_ref_step_golden.npz"))
+def golden_rb(name="rb_ref_step_golden.npz"):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+def golden_steps(g):
+    return int(g["steps"]) if "steps" in g.files else 3
 
 
 def make_ref_system(g, max_pairs=1 << 16):
@@ -41,14 +45,19 @@ def make_ref_system(g, max_pairs=1 << 16):
     return prb, s, dt
 
 
+@pytest.mark.parametrize("fixture", ["rb_ref_step_golden.npz", "rb_demo_steps_golden.npz"])
 @pytest.mark.parametrize("fused", [False, True])
-def test_reference_step_matches_reference_kernels(cuda, fused):
+def test_reference_step_matches_reference_kernels(cuda, fused, fixture):
+    """A 64-body ring scene for 3 steps and the headless demo's scene (two
+    hexagon sizes, 256 bodies in contact) for 4 steps, through the fused
+    step and through the separate entry points in the demo's order."""
     from gsap_gb300 import MODE_SPHERE, Sap
     import oracle
-    g = golden_rb()
+    g = golden_rb(fixture)
     prb, s, dt = make_ref_system(g)
     sap = Sap(len(s["p_pos"]), mode=MODE_SPHERE)
-    for step in range(3):
+    last = golden_steps(g) - 1
+    for step in range(last + 1):
         if fused:
             prb.step(sap, dt)
         else:
@@ -78,8 +87,8 @@ def test_reference_step_matches_reference_kernels(cuda, fused):
     sap.check()
     # the -fmad=false reference kernels reproduce the host-compiled
     # reference kernels exactly
-    assert np.array_equal(st["pos"], g["step2__pos"])
-    assert np.array_equal(st["lin_vel"], g["step2__lin_vel"])
+    assert np.array_equal(st["pos"], g[f"step{last}__pos"])
+    assert np.array_equal(st["lin_vel"], g[f"step{last}__lin_vel"])
 
 
 def test_collision_matches_reference_format(cuda, oracle_lib):

@@ -68,13 +68,16 @@ def test_sap_slices_cover_the_full_sweep(oracle_lib):
     assert got == {tuple(p) for p in full}
 
 
-def test_rb_reference_step_matches_reference_kernels(oracle_lib):
-    """The FP32 restatement reproduces the reference kernels bit for bit."""
-    g = load("rb_ref_step_golden.npz")
+@pytest.mark.parametrize("fixture", ["rb_ref_step_golden.npz", "rb_demo_steps_golden.npz"])
+def test_rb_reference_step_matches_reference_kernels(oracle_lib, fixture):
+    """The FP32 restatement reproduces the reference kernels bit for bit:
+    a 64-body ring scene for 3 steps, and the headless demo's scene (two
+    hexagon sizes, 256 bodies in contact) for 4 steps."""
+    g = load(fixture)
     dt, spM, dpM, vmax, gy = (float(x) for x in g["params"])
     s = {k[len("init__"):]: g[k].copy() for k in g.files if k.startswith("init__")}
     oracle_lib.normalize_quats(s["quat"])  # setRbData's upload normalisation
-    for step in range(3):
+    for step in range(int(g["steps"]) if "steps" in g.files else 3):
         npairs = oracle_lib.rb_step_ref(s, dt, spM, dpM, max_lin_vel=vmax, gravity_y=gy, floor_clamp=True,
                                         torque_quirk=True, pair_loop_quirk=True)
         assert npairs == int(g[f"step{step}__npairs"])
