@@ -417,6 +417,7 @@ static gsap_status validate(gsap_sap* h, const float* mn, const float* mx, uint3
 static gsap_status broadphase(gsap_sap* h, const float* d_min, const float* d_max, const uint32_t* off,
                               uint32_t S, uint32_t n, uint32_t* d_pairs, uint64_t cap, uint64_t* d_count,
                               uint64_t* h_count, uint32_t flags, void* stream) {
+    if (!h) return fail(GSAP_ERR_INVALID, "null handle");
     int mode = (int)h->cfg.mode;
     gsap_status v = validate(h, d_min, d_max, n, mode, d_pairs, S);
     if (v != GSAP_OK) return v;
