@@ -277,8 +277,13 @@ static gsap_status record(gsap_sap* h, const Call& c, cudaStream_t st, bool time
     a.spin_limit = h->cfg.spin_limit;
     const int passes = (int)(a.key_bits / 8);
     int ev = 0;
+    static const char* const kStage[] = {"gsap:pca", "gsap:project", "gsap:sort", "gsap:sweep", "gsap:output"};
+    NvtxRange nv;
+    int stage = 0;
     auto mark = [&]() {
         if (timed) cudaEventRecord(h->ev[ev++], st);
+        if (stage < 5) nv.next(kStage[stage]);
+        ++stage;
     };
     mark();
     const bool temporal = (c.flags & GSAP_FLAG_TEMPORAL) != 0;
@@ -418,6 +423,7 @@ static gsap_status broadphase(gsap_sap* h, const float* d_min, const float* d_ma
                               uint32_t S, uint32_t n, uint32_t* d_pairs, uint64_t cap, uint64_t* d_count,
                               uint64_t* h_count, uint32_t flags, void* stream) {
     if (!h) return fail(GSAP_ERR_INVALID, "null handle");
+    NvtxRange range("gsap:broadphase");
     int mode = (int)h->cfg.mode;
     gsap_status v = validate(h, d_min, d_max, n, mode, d_pairs, S);
     if (v != GSAP_OK) return v;

@@ -2,11 +2,31 @@
 // layers.
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include "../../include/gsap.h"
 
 namespace gsap {
+
+// NVTX ranges for profilers (host-side enqueue of each stage; header-only,
+// no cost without an attached tool).  A range opened here is closed by the
+// next stage or when the object goes out of scope (error returns included).
+struct NvtxRange {
+    int open = 0;
+    NvtxRange() = default;
+    explicit NvtxRange(const char* name) { next(name); }
+    void next(const char* name) {
+        if (open) nvtxRangePop();
+        nvtxRangePushA(name);
+        open = 1;
+    }
+    ~NvtxRange() {
+        if (open) nvtxRangePop();
+    }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 struct BpDeviceCounts {
     const unsigned long long* num_pairs;  // i<j pairs of the last call (device)

@@ -299,6 +299,7 @@ extern "C" gsap_status gsap_rb_set_num_pairs(gsap_rb* h, int32_t num_pairs, int3
 
 extern "C" gsap_status gsap_rb_step(gsap_rb* h, gsap_sap* bp, float dt, void* stream) {
     if (!h || !bp) return set_error(GSAP_ERR_INVALID, "null handle");
+    NvtxRange range("gsap:rb_step");
     cudaStream_t st = (cudaStream_t)stream;
     gsap_status r;
     if (h->cp.model == GSAP_CONTACT_REF) {

@@ -105,6 +105,17 @@ def test_capacity_error_reports_required_size(sap, cuda):
     assert len(out) == 780
 
 
+def test_allocation_failure_is_reported(cuda, oracle_lib):
+    """A handle whose scratch cannot exist (34 TB of pair capacity) is refused
+    at create with a CUDA status and a message, and the device stays usable."""
+    from gsap_gb300 import GsapError, Sap, scenes
+    with pytest.raises(GsapError) as ei:
+        Sap(1000, pair_factor=(1 << 32) - 1)
+    assert "allocation failed" in str(ei.value)
+    mn, mx = scenes.aabb_uniform(4096, 5)
+    assert np.array_equal(run_bp(Sap(4096), mn, mx, cuda), oracle_lib.bf_aabb(mn, mx))
+
+
 def test_nonfinite_input_is_reported(sap, cuda):
     from gsap_gb300 import GsapError
     mn = np.zeros((100, 4), np.float32)
