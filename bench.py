@@ -10,8 +10,17 @@ reference's Sap::collision canonicalises its output.  Synthetic data, seeded.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
-Prints one JSON line (rank 0).  --impl reference times the reference
-algorithm restated on the CPU (oracle/, the checker) on the host cores.
+Prints one JSON line (rank 0): the device-timed throughput (value), the
+same metric end to end through the public API with host copies (e2e), the
+dominant kernel against the measured HBM peak (roofline, with the L1 and
+DRAM throughput of its committed ncu summary), the whole call against
+156 n + 8 P bytes, per-stage times, the restated reference on the host
+cores (cpu_baseline), kernel launches, sampled clocks, and extras (the
+16,384-box case against the O(n^2) brute force, a 16,777,216-box scene,
+4096 batched scenes, the rigid-body step).  --impl reference times the
+reference algorithm restated on the CPU (oracle/, the checker) on all host
+cores: each step one call whose sweeps start from one slice of each sorted
+group, slices in turn, reported as the full-call time they add up to.
 """
 from __future__ import annotations
 
