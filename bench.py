@@ -156,6 +156,14 @@ def dist_setup():
     return world, rank, local
 
 
+def workload_config(args, world: int) -> dict:
+    """The `config` of the JSON line, the same for both arms."""
+    return {"workload": "gauss1m: 1,048,576 AABBs, anisotropic Gaussian std (100,20,5) under a seeded "
+                        "rotation, log-normal half-extents, 64 jittered copies cycled",
+            "n": args.n, "l2": f"inputs cycled over {args.jitter_sets} x {2 * args.n * 16 >> 20} MiB",
+            "output": "sorted (i<j) uint32 pairs", "parallelism": f"replicas x{world}"}
+
+
 def make_inputs(rank: int, n: int, sets_wanted: int = N_JITTER):
     """n objects; for n != 1,048,576 the spread is scaled by (n / 2^20)^(1/3)
     so the object density (and so the work per object) stays that of the
@@ -285,6 +293,39 @@ def run_ours(args, world, rank, local):
     torch.cuda.synchronize()
     unsorted_ms = e0.elapsed_time(e1) / 16
 
+    # Graph mode with new buffers on every call: windows of larger buffers at
+    # a new offset each call (same shape, new pointers).  Once the handle
+    # holds 64 graphs of this shape, each call re-captures its launches and
+    # updates a cached graph in place (cudaGraphExecUpdate).
+    KF = 100
+    big_mn = torch.empty((n + 2 * KF + 160, 4), dtype=torch.float32, device=dev)
+    big_mx = torch.empty_like(big_mn)
+    big_mn[:n] = dsets[0][0]
+    big_mn[n:] = dsets[0][0][: big_mn.shape[0] - n]
+    big_mx[:n] = dsets[0][1]
+    big_mx[n:] = dsets[0][1][: big_mx.shape[0] - n]
+    big_pairs = torch.empty((cap + 2 * KF + 160, 2), dtype=torch.int32, device=dev)
+
+    def fresh(k):
+        sap.broadphase_async(big_mn[k:k + n], big_mx[k:k + n], big_pairs[k:k + cap], d_count, sorted=True,
+                             graph=True, stream=stream)
+
+    for k in range(80):  # fills the per-shape quota (instantiations), then updates
+        fresh(k)
+    torch.cuda.synchronize()
+    sap.check()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    h0 = time.perf_counter()
+    for k in range(80, 80 + KF):
+        fresh(k)
+    host_s = time.perf_counter() - h0
+    f1.record(stream)
+    torch.cuda.synchronize()
+    sap.check()
+    fresh_ms = f0.elapsed_time(f1) / KF
+    del big_mn, big_mx, big_pairs
+
     # End to end through the public API with host buffers, as a streaming
     # user runs it: every call copies its inputs from pinned host memory and
     # reads back its pair count and pair list.  Two slots: the copies of one
@@ -376,20 +417,20 @@ def run_ours(args, world, rank, local):
         "value": round(value, 3), "unit": "Mobjects/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": "gauss1m: 1,048,576 AABBs, anisotropic Gaussian std (100,20,5) under a seeded "
-                               "rotation, log-normal half-extents, 64 jittered copies cycled",
-                   "n": n, "pairs_per_call": P0,
-                   "l2": f"inputs cycled over {len(dsets)} x {2 * n * 16 >> 20} MiB",
-                   "output": "sorted (i<j) uint32 pairs", "parallelism": f"replicas x{world}",
-                   "settings": dict(tuned, autotuned=True) if tuned else
-                   {"sort_bits": args.sort_bits or 32, "cell_factor": args.cell_factor or 2.0, "autotuned": False}},
+        "config": workload_config(args, world),
+        "pairs_per_call": P0,
+        "settings": dict(tuned, autotuned=True) if tuned else
+        {"sort_bits": args.sort_bits or 32, "cell_factor": args.cell_factor or 2.0, "autotuned": False},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": f"stage:{dom}",
                      "peak_kind": peak_kind,
+                     "traffic_source": "from the committed ncu capture of this kernel on this workload "
+                                       "(profiles/ncu_traffic.txt), not measured in this run",
                      # what limits it instead: the L1 data path (one ncu --set full capture)
                      "limiter": {"l1tex_throughput_frac": profile_metric(f"k_{dom}", "L1/TEX Cache Throughput"),
                                  "dram_throughput_frac": profile_metric(f"k_{dom}", "DRAM Throughput"),
-                                 "source": f"profiles/k_{dom}_gauss1m.md"}},
+                                 "source": f"profiles/k_{dom}_gauss1m.md (from the committed capture, "
+                                           "not measured in this run)"}},
         "pipeline_roofline": {"bytes_alg": alg["total"], "achieved_gbs": round(pipe_gbs, 1),
                               "frac": round(pipe_gbs / peak, 4), "formula": "156 n + 8 P"},
         "stage_ms": {k: round(v, 4) for k, v in st_ms.items()},
@@ -397,6 +438,11 @@ def run_ours(args, world, rank, local):
                         "qbits": stats["qbits"], "warp_iters": stats["iters"],
                         "lane_efficiency": round(stats["tests"] / max(1, 32 * stats["iters"]), 3)},
         "unsorted_ms_per_step": round(unsorted_ms, 4),
+        "new_buffers_every_call": {"ms_per_step": round(fresh_ms, 4), "host_ms_per_call": round(host_s / KF * 1e3, 4),
+                                   "calls": KF, "cached_ms_per_step": round(ms, 4),
+                                   "mode": "graph mode, new input and output pointers each call: the launches "
+                                           "are captured again and a cached graph of the shape is updated in "
+                                           "place (cudaGraphExecUpdate)"},
         "temporal": {"ms_per_step": round(temporal_ms, 4), "value": round(n / (temporal_ms / 1e3) / 1e6, 3),
                      "unit": "Mobjects/s",
                      "mode": "GSAP_FLAG_TEMPORAL: grid of the previous call, this call's PCA beside the sweep"},
@@ -450,6 +496,40 @@ def run_extras(args, dev, stream):
                                              and int(scnt.item()) == len(bf))
     out["small_16k"] = small
     del ssap, spairs
+    # --- the reference's own call: Sap::collision on the particles of the
+    # headless demo scene (4096 hexagon bodies x 6 particles = 24,576 spheres,
+    # demoParticles.h:403, :898-903), both-direction list + pairEntries
+    from gsap_gb300 import demo
+    dsc = demo.demo_scene(4096, n_row=16, seed=0)
+    dprb = ParticleRigidBody(4096, dsc["n_particles"], 16)
+    dprb.load_scene(dsc)
+    dprb.update_particle_data()
+    dsph = torch.from_numpy(dprb.get_particles()["p_pos"]).to(dev)
+    nsp = dsph.shape[0]
+    csap = Sap(nsp, mode=1)
+    cpairs = torch.empty((40 * nsp, 2), dtype=torch.int32, device=dev)
+    cent = torch.empty(nsp + 1, dtype=torch.int32, device=dev)
+    for _ in range(5):
+        npc, nec = csap.collision(0.0, dsph, cpairs, cent, stream=stream)
+    h0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(100):
+        npc, nec = csap.collision(0.0, dsph, cpairs, cent, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    coll = {"spheres": nsp, "pairs_both_directions": npc, "pair_entries": nec,
+            "ms_per_call": round((time.perf_counter() - h0) * 10, 4),
+            "device_ms_per_call": round(e0.elapsed_time(e1) / 100, 4),
+            "note": "gsap_sap_collision blocks for the host counts each call, as Sap::collision does"}
+    if not args.no_cpu:
+        import oracle
+        sp = dsph.cpu().numpy()
+        wp, we = oracle.both_directions(oracle.bf_sphere(sp))
+        coll["equal_to_brute_force"] = bool(npc == len(wp) and nec == len(we) and
+                                            np.array_equal(cpairs[:npc].cpu().numpy(), wp) and
+                                            np.array_equal(cent[:nec].cpu().numpy(), we))
+    out["demo_collision_24k"] = coll
+    del dprb, csap, cpairs, cent
     # --- large case: 16,777,216 AABBs at the 1M workload's object density
     # (spread scaled by 16^(1/3)); one input set of 512 MiB, larger than L2
     nl = 1 << 24
@@ -482,14 +562,15 @@ def run_extras(args, dev, stream):
     n = len(mn)
     dmn, dmx = torch.from_numpy(mn).to(dev), torch.from_numpy(mx).to(dev)
     doff = torch.from_numpy(off.astype(np.int32)).to(dev)
-    bsap = Sap(n, max_scenes=S)
-    cap = 8 * n
+    bsap = Sap(n, max_scenes=S, pair_factor=2)
+    cap = 2 * n
     pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
     cnt = torch.zeros(1, dtype=torch.int64, device=dev)
     import ctypes as C
 
     from gsap_gb300 import _lib
     L = _lib.load()
+    btuned = bsap.autotune(dmn, dmx, offsets=doff, pairs=pairs, sorted=True, graph=True, reps=3, stream=stream)
 
     def batched_call():
         st = L.gsap_broadphase_batched(bsap.handle, dmn.data_ptr(), dmx.data_ptr(), doff.data_ptr(), S, n,
@@ -502,6 +583,12 @@ def run_extras(args, dev, stream):
     torch.cuda.synchronize()
     bsap.check()
     Pb = int(cnt.item())
+    equal = None
+    if not args.no_cpu:
+        import oracle
+        want = oracle.pairs_batched(mn, mx, off, bf_max=8192)
+        got = pairs[:Pb].cpu().numpy().astype(np.uint32)
+        equal = bool(len(got) == len(want) and np.array_equal(got, want))
     reps = 5
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -534,39 +621,62 @@ def run_extras(args, dev, stream):
                       "plain_scenes_per_s": round(S / (plain_ms / 1e3), 1),
                       "speedup_vs_plain": round(plain_ms / batched_ms, 2),
                       "achieved_gbs": round(bbytes / (batched_ms / 1e3) / 1e9, 1),
-                      "frac": round(bbytes / (batched_ms / 1e3) / 1e9 / peak, 4)}
-    del bsap, pairs, dmn, dmx
+                      "frac": round(bbytes / (batched_ms / 1e3) / 1e9 / peak, 4),
+                      "settings": dict(btuned, autotuned=True),
+                      "equal_to_reference": equal,
+                      "reference": "oracle per scene: O(n^2) Aabb::overlaps for scenes <= 8192 objects, the same "
+                                   "predicate on x-overlapping pairs above (untimed check of the timed output)"}
+    del bsap, psap, pairs, dmn, dmx
     torch.cuda.empty_cache()
+
     # --- rigid body: 65,536 cubes of 2x2x2 particles in a 200^3 box, 1000 steps
+    dt = 1.0 / 600.0
     nb = args.bodies
     sc = scenes.cubes_in_box(nb, box=200.0, seed=3)
     cfgp = dict(k=2e4, eta=50.0, kt=0.1, gravity_y=-9.81, box_lo=(0.0, 0.0, 0.0), box_hi=(200.0, 200.0, 200.0))
     prb = ParticleRigidBody(nb, sc["n_particles"], 16)
     prb.load_scene(sc)
     prb.set_contact(model=CONTACT_CONFIG, **cfgp)
+    init = {k: np.ascontiguousarray(sc[k], np.float32) for k in ("pos", "quat", "lin_vel", "ang_vel")}
     rsap = Sap(nb, sort_bits=24)  # the key width the autotuner picks for the 1M scene
-    dt = 1.0 / 600.0
-    # one step from the initial state against the FP64 oracle (CPU)
-    err = None
+    rb = {"bodies": nb, "particles": sc["n_particles"]}
     if not args.no_cpu:
         import oracle
-        oracle.build()
+        from oracle.trajectory import fp64_errors
         st64 = scenes.to_f64(sc)
         t0 = time.perf_counter()
         oracle.rb_step_cfg_f64(st64, dict(cfgp, dt=dt))
         cpu_rb_s = time.perf_counter() - t0
-        prb.step(rsap, dt, stream=stream)
-        torch.cuda.synchronize()
-        g = prb.get_state()
-
-        def rel(a, b):
-            return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-30))
-        err = {"pos": rel(g["pos"][:, :3], st64["pos"][:, :3]), "vel": rel(g["lin_vel"][:, :3], st64["lin_vel"][:, :3])}
-        prb.load_scene(sc)
+        t0 = time.perf_counter()
+        e = fp64_errors(prb, rsap, sc, dict(cfgp, dt=dt), steps=args.rb_check_steps, stream=stream)
+        rb["fp64_error"] = {"steps": e["steps"], "per_step_max": e["per_step_max"],
+                            "free_running": e["free_running"], "check_s": round(time.perf_counter() - t0, 1),
+                            "definition": "max |gpu - fp64| / max |fp64| over xyz; per step: each GPU step "
+                                          "taken from the FP64 state rounded to FP32; free running: the GPU's "
+                                          "own trajectory after all steps"}
+        rb["cpu_baseline"] = {"value": round(nb / cpu_rb_s / 1e6, 4), "unit": "Mbody_steps/s",
+                              "cores": os.cpu_count(), "kind": "port",
+                              "sample": "one config-model step of the same scene, FP64 oracle "
+                                        "(oracle/rb.c orc_rb_step_cfg_f64, OpenMP)"}
+    prb.set_state(init)
     for _ in range(5):
         prb.step(rsap, dt, stream=stream)
     torch.cuda.synchronize()
     rsap.check()
+    # step split: broadphase stages (CUDA events inside the step) against the whole step, eager launches
+    rsap.enable_timing(True)
+    split = []
+    for _ in range(10):
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        prb.step(rsap, dt, stream=stream)
+        s1.record(stream)
+        torch.cuda.synchronize()
+        split.append((s0.elapsed_time(s1), sum(rsap.stage_times())))
+    rsap.enable_timing(False)
+    prb.set_state(init)
+    prb.step(rsap, dt, stream=stream)
+    torch.cuda.synchronize()
     Pb_rb = int(rsap.stats()["pairs"])
     # one step captured as a CUDA graph (the step makes no host synchronisation)
     gstream = torch.cuda.Stream()
@@ -577,6 +687,7 @@ def run_extras(args, dev, stream):
         graph.replay()
     torch.cuda.synchronize()
     rsap.check()
+    prb.contacts(reset=True)
     steps = 1000
     e0.record(stream)
     for _ in range(steps):
@@ -585,21 +696,23 @@ def run_extras(args, dev, stream):
     torch.cuda.synchronize()
     rsap.check()
     rb_ms = e0.elapsed_time(e1) / steps
+    Pc = prb.contacts() / (2.0 * steps)  # contact pairs per step (each contact is counted from both sides)
     npart = sc["n_particles"]
-    b_rb = rb_algorithmic_bytes(nb, npart, 64 * Pb_rb, Pb_rb)
-    rb = {"bodies": nb, "particles": npart, "steps": steps, "ms_per_step": round(rb_ms, 4),
-          "launch": "one step captured as a CUDA graph, replayed",
-          "body_steps_per_s": round(nb / (rb_ms / 1e3), 1), "body_pairs": Pb_rb,
-          "bytes_alg": b_rb, "achieved_gbs": round(b_rb / (rb_ms / 1e3) / 1e9, 1),
-          "frac": round(b_rb / (rb_ms / 1e3) / 1e9 / peak, 4),
-          "formula": "276 n_b + 96 n_p + 8 P_c + B_bp(n_b, P_b), P_c = 64 P_b particle pairs tested"}
-    if err is not None:
-        rb["step1_rel_err_vs_fp64"] = err
-        rb["cpu_baseline"] = {"value": round(nb / cpu_rb_s / 1e6, 4), "unit": "Mbody_steps/s", "cores": os.cpu_count(),
-                              "kind": "port", "sample": "one config-model step of the same scene, FP64 oracle "
-                                                        "(oracle/rb.c orc_rb_step_cfg_f64, OpenMP)"}
+    b_rb = rb_algorithmic_bytes(nb, npart, int(Pc), Pb_rb)
+    step_ms, bp_ms = float(np.median([a for a, _ in split])), float(np.median([b for _, b in split]))
+    rb.update({"steps": steps, "ms_per_step": round(rb_ms, 4),
+               "launch": "one step captured as a CUDA graph, replayed",
+               "body_steps_per_s": round(nb / (rb_ms / 1e3), 1), "body_pairs": Pb_rb,
+               "contact_pairs_per_step": round(Pc, 1),
+               "bytes_alg": b_rb, "achieved_gbs": round(b_rb / (rb_ms / 1e3) / 1e9, 1),
+               "frac": round(b_rb / (rb_ms / 1e3) / 1e9 / peak, 4),
+               "formula": "276 n_b + 96 n_p + 8 P_c + B_bp(n_b, P_b), P_c = particle contact pairs per step "
+                          "(device counter of the force kernel)",
+               "step_split_eager_ms": {"step": round(step_ms, 4), "broadphase": round(bp_ms, 4),
+                                       "rigid_kernels_and_gaps": round(step_ms - bp_ms, 4),
+                                       "note": "10 eager steps, CUDA events; the timed graph replay has no gaps"}})
     out["rigid"] = rb
-    del prb, rsap
+    del prb, rsap, graph
     torch.cuda.empty_cache()
 
     # --- batched dynamics: 1024 scenes of 256..8192 bodies (cubes, rods, L shapes) in a 100^3 box
@@ -611,20 +724,44 @@ def run_extras(args, dev, stream):
     bprb.load_scene(ms_)
     bprb.set_contact(model=CONTACT_CONFIG, **cfgb)
     bprb.set_scenes(bo)
+    binit = {k: np.ascontiguousarray(ms_[k], np.float32) for k in ("pos", "quat", "lin_vel", "ang_vel")}
     bsap2 = Sap(nbb, max_scenes=args.rb_scenes)
+    rbb = {"scenes": args.rb_scenes, "bodies": nbb, "particles": ms_["n_particles"]}
+    if not args.no_cpu:
+        from oracle.trajectory import fp64_errors
+        t0 = time.perf_counter()
+        e = fp64_errors(bprb, bsap2, ms_, dict(cfgb, dt=dt), steps=args.rb_check_steps,
+                        check_scenes=min(args.rb_check_scenes, args.rb_scenes), stream=stream)
+        rbb["fp64_error"] = {"steps": e["steps"], "checked_scenes": min(args.rb_check_scenes, args.rb_scenes),
+                             "checked_bodies": e["checked_bodies"], "per_step_max": e["per_step_max"],
+                             "free_running": e["free_running"], "check_s": round(time.perf_counter() - t0, 1),
+                             "definition": "as rigid.fp64_error, over the bodies of the first checked_scenes "
+                                           "scenes of the batch (scenes never interact, so the oracle run on "
+                                           "them alone gives their whole-batch result)"}
+    bprb.set_state(binit)
     for _ in range(3):
         bprb.step(bsap2, dt, stream=stream)
     torch.cuda.synchronize()
     bsap2.check()
+    bgraph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(bgraph, stream=gstream):
+        bprb.step(bsap2, dt, stream=gstream)
+    for _ in range(3):
+        bgraph.replay()
+    torch.cuda.synchronize()
+    bsap2.check()
+    bprb.contacts(reset=True)
     bsteps = 100
     e0.record(stream)
     for _ in range(bsteps):
-        bprb.step(bsap2, dt, stream=stream)
+        bgraph.replay()
     e1.record(stream)
     torch.cuda.synchronize()
     bsap2.check()
     b_ms = e0.elapsed_time(e1) / bsteps
-    # plain: the first 32 scenes, one system per scene, stepped one after another
+    bPc = bprb.contacts() / (2.0 * bsteps)
+    del bgraph
+    # plain: the first 32 scenes, one system per scene, stepped one after another (eager launches)
     nplain = 32
     plain = []
     for s in range(nplain):
@@ -645,12 +782,13 @@ def run_extras(args, dev, stream):
     e1.record(stream)
     torch.cuda.synchronize()
     p_ms = e0.elapsed_time(e1) / psteps
-    out["rigid_batched"] = {"scenes": args.rb_scenes, "bodies": nbb, "particles": ms_["n_particles"],
-                            "ms_per_step": round(b_ms, 4),
-                            "scene_steps_per_s": round(args.rb_scenes / (b_ms / 1e3), 1),
-                            "plain_scene_steps_per_s": round(nplain / (p_ms / 1e3), 1),
-                            "plain_sample": f"first {nplain} scenes, one system each, stepped in turn",
-                            "speedup_vs_plain": round((args.rb_scenes / b_ms) / (nplain / p_ms), 2)}
+    rbb.update({"ms_per_step": round(b_ms, 4), "launch": "one batched step captured as a CUDA graph, replayed",
+                "scene_steps_per_s": round(args.rb_scenes / (b_ms / 1e3), 1),
+                "contact_pairs_per_step": round(bPc, 1),
+                "plain_scene_steps_per_s": round(nplain / (p_ms / 1e3), 1),
+                "plain_sample": f"first {nplain} scenes, one system each, stepped in turn (eager launches)",
+                "speedup_vs_plain": round((args.rb_scenes / b_ms) / (nplain / p_ms), 2)})
+    out["rigid_batched"] = rbb
     return out
 
 
@@ -668,7 +806,7 @@ def run_reference(args, world, rank):
     import oracle
     oracle.build()
     n = args.n
-    host_sets, _ = make_inputs(0, n, min(args.jitter_sets, 8))
+    host_sets, _ = make_inputs(0, n, args.jitter_sets)
     mn, mx = host_sets[0]
     t0 = time.perf_counter()
     _, f1, v1 = oracle.sap_ref_sampled(0, mn, mx, 1, 0)
@@ -702,10 +840,12 @@ def run_reference(args, world, rank):
         "value": round(value, 4), "unit": "Mobjects/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": "gauss1m: 1,048,576 AABBs, anisotropic Gaussian std (100,20,5) under a seeded "
-                               "rotation, log-normal half-extents, 64 jittered copies cycled", "n": n},
+        "config": workload_config(args, world),
         "cpu_baseline": {"value": round(value, 4), "unit": "Mobjects/s", "cores": cores, "kind": "port",
-                         "sample": sample},
+                         "sample": sample, "fixed_ms": round(float(np.mean(fixed)) * 1e3, 3),
+                         "scaled_ms": round(parts * float(np.mean(scaled)) * 1e3, 3),
+                         "split": "fixed = centres, axis choice, partition, group sorts; scaled = the sweeps "
+                                  "and the sort + unique of their pairs (all OpenMP-parallel)"},
         "e2e": {"value": round(value, 4), "unit": "Mobjects/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     return line
@@ -721,6 +861,10 @@ def main():
     ap.add_argument("--scenes", type=int, default=4096)
     ap.add_argument("--bodies", type=int, default=65536)
     ap.add_argument("--rb-scenes", type=int, default=1024)
+    ap.add_argument("--rb-check-steps", type=int, default=100,
+                    help="steps of the FP64 trajectory checks of the rigid-body extras")
+    ap.add_argument("--rb-check-scenes", type=int, default=128,
+                    help="scenes of the batched dynamics checked against the FP64 oracle")
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cell-factor", type=float, default=None,

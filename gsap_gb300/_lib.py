@@ -64,6 +64,7 @@ SIGNATURES = [
     ("gsap_sap_enable_timing", None, [P, C.c_int]),
     ("gsap_sap_autotune", I32, [P, P, P, P, U32, U32, P, U64, U32, C.c_int, C.POINTER(Config), P]),
     ("gsap_radix_sort_u32", I32, [P, P, P, U32, U32, P]),
+    ("gsap_radix_sort_f32", I32, [P, P, P, U32, U32, C.c_int, P]),
     ("gsap_radix_sort_u32_noalloc", I32, [P, P, U32, U32, P]),
     ("gsap_rb_create", P, [I32, I32, I32]),
     ("gsap_rb_destroy", None, [P]),
@@ -85,6 +86,7 @@ SIGNATURES = [
     ("gsap_rb_particle_force", P, [P]),
     ("gsap_rb_step", I32, [P, P, F32, P]),
     ("gsap_rb_get_state", I32, [P, P, P, P, P, P]),
+    ("gsap_rb_set_state", I32, [P, P, P, P, P, P]),
     ("gsap_rb_copy_out", I32, [P, I32, P, U64, P]),
     ("gsap_rb_copy_in", I32, [P, I32, P, U64, P]),
     ("gsap_k_integrate", I32, [P, P, P, P, F32, I32, C.POINTER(ContactParams), P]),
@@ -98,6 +100,8 @@ SIGNATURES = [
     ("gsap_debug_lookback_timeout", C.c_int, [P, U32, P]),
     ("gsap_debug_stats", C.c_int, [P, C.POINTER(U64), P]),
     ("gsap_debug_sizes", C.c_int, [C.POINTER(U32)]),
+    ("gsap_debug_rb_contacts", C.c_int, [P, C.POINTER(U64), C.c_int, P]),
+    ("gsap_debug_graph_cache", C.c_int, [P, U32, C.POINTER(U32)]),
 ]
 
 _LIB = None

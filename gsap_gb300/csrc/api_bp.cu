@@ -53,14 +53,14 @@ gsap_status gsap::set_error(gsap_status st, const char* msg) { return fail(st, "
 
 namespace gsap {
 int sm_count() {
-    static int n = 0;
-    if (n == 0) {
-        int dev = 0;
+    static std::once_flag once[kMaxDevices];
+    static int val[kMaxDevices];
+    return per_device(once, val, [] {
+        int dev = 0, n = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n <= 0) n = 1;
-    }
-    return n;
+        return n > 0 ? n : 1;
+    });
 }
 }  // namespace gsap
 
@@ -79,12 +79,22 @@ extern "C" void gsap_config_default(gsap_config* c) {
 
 // ------------------------------------------------------------------ handle
 
-struct GraphKey {
-    const void *mn, *mx, *off, *pairs, *dcount, *entries;
+// A cached pipeline graph is keyed by its shape (sizes, flags, settings) and
+// by the caller's buffers.  A call whose buffers are new but whose shape is
+// cached captures the launch sequence again and updates an instantiated
+// graph of that shape in place (cudaGraphExecUpdate) once kPerShape graphs
+// of the shape exist, instead of instantiating yet another one.
+struct GraphShape {
     uint32_t n, S, flags, mode, both;
     uint32_t key_bits;
     float cell_factor;
+    uint32_t pad;
     uint64_t cap, ecap;
+    bool operator==(const GraphShape& o) const { return memcmp(this, &o, sizeof(*this)) == 0; }
+};
+struct GraphKey {
+    GraphShape shape;
+    const void *mn, *mx, *off, *pairs, *dcount, *entries;
     bool operator==(const GraphKey& o) const { return memcmp(this, &o, sizeof(*this)) == 0; }
 };
 
@@ -94,6 +104,7 @@ struct GraphEntry {
     uint64_t last_use;
 };
 constexpr size_t kMaxGraphs = 128;  // cached pipeline graphs per handle (LRU)
+constexpr size_t kPerShape = 64;    // graphs of one shape before new buffers update one in place
 
 struct gsap_sap {
     gsap_config cfg;
@@ -103,9 +114,9 @@ struct gsap_sap {
     cudaStream_t cap_stream;
     std::vector<GraphEntry>* graphs;
     uint64_t use_clock;
+    size_t per_shape;   // graphs of one shape kept before new buffers update one (default kPerShape)
     bool timing;
     cudaEvent_t ev[8];
-    float stage_ms[6];
     int nstages;
     // temporal mode: a side stream for the PCA branch, and what the
     // parameters in the scratch were last computed for
@@ -155,6 +166,7 @@ extern "C" gsap_sap* gsap_sap_create(uint32_t max_n, const gsap_config* cfg) {
     memset(h, 0, sizeof(*h));
     h->cfg = c;
     h->graphs = new std::vector<GraphEntry>();
+    h->per_shape = kPerShape;
     cudaGetDevice(&h->device);
     BpScratch& s = h->s;
     s.max_n = max_n;
@@ -220,8 +232,10 @@ extern "C" void gsap_sap_enable_timing(gsap_sap* h, int enable) {
 
 extern "C" int gsap_sap_stage_times(gsap_sap* h, float* out, int max_stages) {
     if (!h || !out) return 0;
+    if (h->nstages > 0 && cudaEventSynchronize(h->ev[h->nstages]) != cudaSuccess) return 0;
     int k = 0;
-    for (; k < h->nstages && k < max_stages; ++k) out[k] = h->stage_ms[k];
+    for (; k < h->nstages && k < max_stages; ++k)
+        if (cudaEventElapsedTime(&out[k], h->ev[k], h->ev[k + 1]) != cudaSuccess) return k;
     return k;
 }
 
@@ -343,34 +357,60 @@ static gsap_status run(gsap_sap* h, const Call& c, cudaStream_t st) {
     GraphKey k;
     memset(&k, 0, sizeof(k));
     k.mn = c.mn; k.mx = c.mx; k.off = c.off; k.pairs = c.pairs; k.dcount = c.d_count; k.entries = c.entries;
-    k.n = c.n; k.S = c.S; k.flags = c.flags; k.mode = (uint32_t)c.mode; k.both = (uint32_t)c.both;
-    k.cap = c.cap; k.ecap = c.ecap;
-    k.key_bits = h->cfg.sort_bits; k.cell_factor = h->cfg.cell_factor;  // tuned settings are baked into a graph
+    GraphShape& sh = k.shape;
+    sh.n = c.n; sh.S = c.S; sh.flags = c.flags; sh.mode = (uint32_t)c.mode; sh.both = (uint32_t)c.both;
+    sh.cap = c.cap; sh.ecap = c.ecap;
+    sh.key_bits = h->cfg.sort_bits; sh.cell_factor = h->cfg.cell_factor;  // tuned settings are baked into a graph
     // LRU cache of captured pipelines, one per (inputs, outputs, sizes, flags)
     GraphEntry* hit = nullptr;
-    for (auto& g : *h->graphs)
+    size_t same = 0;
+    GraphEntry* lru_same = nullptr;  // least recently used graph of this shape
+    for (auto& g : *h->graphs) {
         if (g.key == k) { hit = &g; break; }
-    if (!hit) {
-        if (h->graphs->size() >= kMaxGraphs) {
-            size_t old = 0;
-            for (size_t i = 1; i < h->graphs->size(); ++i)
-                if ((*h->graphs)[i].last_use < (*h->graphs)[old].last_use) old = i;
-            cudaGraphExecDestroy((*h->graphs)[old].exec);
-            h->graphs->erase(h->graphs->begin() + old);
+        if (g.key.shape == sh) {
+            ++same;
+            if (!lru_same || g.last_use < lru_same->last_use) lru_same = &g;
         }
+    }
+    if (!hit) {
         cudaGraph_t g;
         CK(cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal));
         gsap_status r = record(h, c, h->cap_stream, false);
         cudaError_t e = cudaStreamEndCapture(h->cap_stream, &g);
         if (r != GSAP_OK) return r;
         if (e != cudaSuccess) return fail(GSAP_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
-        GraphEntry ent;
-        ent.key = k;
-        e = cudaGraphInstantiate(&ent.exec, g, 0);
+        if (same >= h->per_shape) {
+            // new buffers, known shape: the same launches with other pointers
+            cudaGraphExecUpdateResultInfo info;
+            e = cudaGraphExecUpdate(lru_same->exec, g, &info);
+            if (e == cudaSuccess) {
+                lru_same->key = k;
+                hit = lru_same;
+            } else {  // topology differs after all: replace that graph
+                cudaGetLastError();
+                cudaGraphExecDestroy(lru_same->exec);
+                h->graphs->erase(h->graphs->begin() + (lru_same - h->graphs->data()));
+            }
+        }
+        if (!hit) {
+            if (h->graphs->size() >= kMaxGraphs) {
+                size_t old = 0;
+                for (size_t i = 1; i < h->graphs->size(); ++i)
+                    if ((*h->graphs)[i].last_use < (*h->graphs)[old].last_use) old = i;
+                cudaGraphExecDestroy((*h->graphs)[old].exec);
+                h->graphs->erase(h->graphs->begin() + old);
+            }
+            GraphEntry ent;
+            ent.key = k;
+            e = cudaGraphInstantiate(&ent.exec, g, 0);
+            if (e != cudaSuccess) {
+                cudaGraphDestroy(g);
+                return fail(GSAP_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+            }
+            h->graphs->push_back(ent);
+            hit = &h->graphs->back();
+        }
         cudaGraphDestroy(g);
-        if (e != cudaSuccess) return fail(GSAP_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
-        h->graphs->push_back(ent);
-        hit = &h->graphs->back();
     }
     hit->last_use = ++h->use_clock;
     CK(cudaGraphLaunch(hit->exec, st));
@@ -381,8 +421,6 @@ static gsap_status run(gsap_sap* h, const Call& c, cudaStream_t st) {
 static gsap_status finish(gsap_sap* h, cudaStream_t st, uint64_t* count_out, uint64_t cap) {
     CK(cudaMemcpyAsync(h->h_ctrl, h->s.ctrl, 24, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    if (h->timing)
-        for (int k = 0; k < h->nstages; ++k) cudaEventElapsedTime(&h->stage_ms[k], h->ev[k], h->ev[k + 1]);
     uint32_t err = h->h_ctrl[0];
     uint64_t cnt;
     memcpy(&cnt, (char*)h->h_ctrl + 16, 8);
@@ -592,24 +630,27 @@ extern "C" gsap_status gsap_sap_scene_axes(gsap_sap* h, uint32_t scene, double* 
     return GSAP_OK;
 }
 
-extern "C" gsap_status gsap_radix_sort_u32(gsap_sap* h, uint32_t* d_keys, uint32_t* d_vals, uint32_t n,
-                                           uint32_t bits, void* stream) {
-    if (!h || (!d_keys && n)) return fail(GSAP_ERR_INVALID, "null argument");
+// The standalone onesweep sort on a handle's scratch.  flip: the keys are
+// floats, sorted through their order-preserving uint32 images (mapped as
+// the first pass loads them, mapped back as the last pass stores them).
+static gsap_status handle_sort(gsap_sap* h, uint32_t* d_keys, uint32_t* d_vals, uint32_t n, uint32_t bits, int flip,
+                               void* stream) {
     if (n > h->s.entry_cap) return fail(GSAP_ERR_CAPACITY, "n = %u exceeds the sort capacity %llu", n, (unsigned long long)h->s.entry_cap);
-    if (bits == 0 || bits > 32) return fail(GSAP_ERR_INVALID, "bits must be in 1..32");
     if (n < 2) return GSAP_OK;
     cudaStream_t st = (cudaStream_t)stream;
     BpScratch& s = h->s;
     const int passes = (int)((bits + 7) / 8);
     uint32_t* count = &s.ctrl->sort_n;
-    CK(launch_sort_prep(s, d_keys, count, n, passes, st));
+    CK(launch_sort_prep(s, d_keys, count, n, passes, st, flip));
     uint32_t* vals = d_vals ? d_vals : s.vals[0];
     if (!d_vals) CK(cudaMemsetAsync(vals, 0, 4ull * n, st));
     uint32_t* kb[2] = {d_keys, s.keys[1]};
     uint32_t* vb[2] = {vals, s.vals[1]};
     int src = 0;
     for (int p = 0; p < passes; ++p) {
-        CK(launch_sort_pass(s, p, passes, kb[src], vb[src], kb[src ^ 1], vb[src ^ 1], count, n, h->cfg.spin_limit, st));
+        const int fmode = flip ? ((p == 0 ? kSortFlipIn : 0) | (p == passes - 1 ? kSortUnflipOut : 0)) : 0;
+        CK(launch_sort_pass(s, p, passes, kb[src], vb[src], kb[src ^ 1], vb[src ^ 1], count, n, h->cfg.spin_limit, st,
+                            nullptr, false, fmode));
         src ^= 1;
     }
     if (src) {
@@ -617,6 +658,22 @@ extern "C" gsap_status gsap_radix_sort_u32(gsap_sap* h, uint32_t* d_keys, uint32
         if (d_vals) CK(cudaMemcpyAsync(d_vals, vb[1], 4ull * n, cudaMemcpyDeviceToDevice, st));
     }
     return finish(h, st, nullptr, ~0ull);
+}
+
+extern "C" gsap_status gsap_radix_sort_u32(gsap_sap* h, uint32_t* d_keys, uint32_t* d_vals, uint32_t n,
+                                           uint32_t bits, void* stream) {
+    if (!h || (!d_keys && n)) return fail(GSAP_ERR_INVALID, "null argument");
+    if (bits == 0 || bits > 32) return fail(GSAP_ERR_INVALID, "bits must be in 1..32");
+    return handle_sort(h, d_keys, d_vals, n, bits, 0, stream);
+}
+
+extern "C" gsap_status gsap_radix_sort_f32(gsap_sap* h, float* d_keys, uint32_t* d_vals, uint32_t n,
+                                           uint32_t key_bits, int negative_keys, void* stream) {
+    if (!h || (!d_keys && n)) return fail(GSAP_ERR_INVALID, "null argument");
+    if (key_bits == 0 || key_bits > 32) return fail(GSAP_ERR_INVALID, "key_bits must be in 1..32");
+    if (negative_keys && key_bits != 32)
+        return fail(GSAP_ERR_INVALID, "signed float keys are sorted on all 32 bits (key_bits must be 32)");
+    return handle_sort(h, reinterpret_cast<uint32_t*>(d_keys), d_vals, n, key_bits, negative_keys ? 1 : 0, stream);
 }
 
 // ------------------------------------------------------------ debug hooks
@@ -684,6 +741,13 @@ extern "C" int gsap_debug_lookback_timeout(gsap_sap* h, uint32_t spin_limit, voi
     return finish(h, st, nullptr, ~0ull);
 }
 
+extern "C" int gsap_debug_graph_cache(gsap_sap* h, uint32_t per_shape, uint32_t* out_count) {
+    if (!h) return -1;
+    if (per_shape) h->per_shape = per_shape;
+    if (out_count) *out_count = (uint32_t)h->graphs->size();
+    return 0;
+}
+
 extern "C" int gsap_debug_sizes(uint32_t* out) {
     if (!out) return -1;
     out[0] = sizeof(Ctrl);
@@ -725,7 +789,9 @@ gsap_status gsap::bp_both_async(gsap_sap* h, int mode, const float4* mn, const f
         CK(cudaMemsetAsync(h->s.rowoff, 0, 4ull * (n + 1), st));
         return GSAP_OK;
     }
-    gsap_status r = record(h, c, st, false);
+    // with timing enabled the stages of this call are timed too (a step
+    // that is not graph-captured; gsap_sap_stage_times reads them)
+    gsap_status r = record(h, c, st, h->timing);
     if (r == GSAP_OK) temporal_note(h, c);
     return r;
 }

@@ -18,6 +18,14 @@
 // Set-up: the first call on each device looks the array up with
 // cudaGetSymbolAddress and zeroes its control block and look-back words
 // (synchronously).  Make that first call before any stream capture begins.
+// Later calls look the address up again (this allocates nothing); a failed
+// set-up is not remembered, so the next call retries it, and an address
+// that changed (the module was loaded again after cudaDeviceReset) gets a
+// fresh set-up.
+//
+// Pointers: the keys and values must be device memory of the current
+// device; memory of another device, or host memory CUDA does not know,
+// is rejected with GSAP_ERR_INVALID before anything runs.
 //
 // What must start at zero: the control block (error word, tile counters,
 // digit histograms, epoch) and the look-back words.  Set-up zeroes them;
@@ -52,13 +60,53 @@ constexpr uint64_t kBytes = kOffVals0 + up(4ull * kMaxN);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kBytes];
 
-constexpr int kMaxDevices = 64;
 struct Slot {
-    std::once_flag once;
-    unsigned char* base = nullptr;
-    cudaError_t err = cudaSuccess;
+    std::mutex mu;
+    unsigned char* base = nullptr;  // set only once a set-up succeeded for this address
 };
 Slot g_slots[kMaxDevices];
+
+// The array's device address on device `dev` (current), set up on first use.
+cudaError_t scratch_base(int dev, unsigned char** out) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    Slot& slot = g_slots[dev];
+    std::lock_guard<std::mutex> lock(slot.mu);
+    if (slot.base != (unsigned char*)p) {
+        slot.base = nullptr;
+        e = cudaMemset(p, 0, kZeroBytes);
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) return e;
+        slot.base = (unsigned char*)p;
+    }
+    *out = slot.base;
+    return cudaSuccess;
+}
+
+// GSAP_OK when p is device (or managed) memory usable on device `dev`.
+gsap_status check_ptr(const void* p, int dev, const char* what) {
+    if (!p) return GSAP_OK;
+    cudaPointerAttributes a;
+    cudaError_t e = cudaPointerGetAttributes(&a, p);
+    char buf[192];
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        snprintf(buf, sizeof(buf), "gsap_radix_sort_u32_noalloc: %s is not a CUDA pointer (%s)", what,
+                 cudaGetErrorString(e));
+        return set_error(GSAP_ERR_INVALID, buf);
+    }
+    if (a.type == cudaMemoryTypeUnregistered) {
+        snprintf(buf, sizeof(buf), "gsap_radix_sort_u32_noalloc: %s is host memory unknown to CUDA", what);
+        return set_error(GSAP_ERR_INVALID, buf);
+    }
+    if (a.type == cudaMemoryTypeDevice && a.device != dev) {
+        snprintf(buf, sizeof(buf), "gsap_radix_sort_u32_noalloc: %s is on device %d, the current device is %d", what,
+                 a.device, dev);
+        return set_error(GSAP_ERR_INVALID, buf);
+    }
+    return GSAP_OK;
+}
 
 gsap_status cuda_fail(cudaError_t e, const char* what) {
     char buf[256];
@@ -84,25 +132,22 @@ extern "C" gsap_status gsap_radix_sort_u32_noalloc(uint32_t* d_keys, uint32_t* d
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
     if (dev < 0 || dev >= kMaxDevices) return set_error(GSAP_ERR_INVALID, "gsap_radix_sort_u32_noalloc: device ordinal out of range");
-    Slot& slot = g_slots[dev];
-    std::call_once(slot.once, [&slot]() {
-        void* p = nullptr;
-        slot.err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (slot.err == cudaSuccess) slot.err = cudaMemset(p, 0, kZeroBytes);
-        if (slot.err == cudaSuccess) slot.err = cudaDeviceSynchronize();
-        if (slot.err == cudaSuccess) slot.base = (unsigned char*)p;
-    });
-    if (!slot.base) return cuda_fail(slot.err, "set-up of the static scratch");
+    gsap_status pc = check_ptr(d_keys, dev, "keys");
+    if (pc == GSAP_OK) pc = check_ptr(d_vals, dev, "values");
+    if (pc != GSAP_OK) return pc;
+    unsigned char* base = nullptr;
+    e = scratch_base(dev, &base);
+    if (e != cudaSuccess) return cuda_fail(e, "set-up of the static scratch");
 
     BpScratch s{};
-    s.ctrl = (Ctrl*)(slot.base + kOffCtrl);
-    s.status = (uint64_t*)(slot.base + kOffStatus);
+    s.ctrl = (Ctrl*)(base + kOffCtrl);
+    s.status = (uint64_t*)(base + kOffStatus);
     s.status_words = kTiles * 256ull;
     s.entry_cap = kMaxN;
     s.max_n = kMaxN;
-    uint32_t* keys_alt = (uint32_t*)(slot.base + kOffKeys);
-    uint32_t* vals_alt = (uint32_t*)(slot.base + kOffVals);
-    uint32_t* vals0 = (uint32_t*)(slot.base + kOffVals0);
+    uint32_t* keys_alt = (uint32_t*)(base + kOffKeys);
+    uint32_t* vals_alt = (uint32_t*)(base + kOffVals);
+    uint32_t* vals0 = (uint32_t*)(base + kOffVals0);
 
     cudaStream_t st = (cudaStream_t)stream;
     const int passes = (int)((bits + 7) / 8);

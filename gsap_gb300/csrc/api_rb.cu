@@ -49,12 +49,13 @@ struct gsap_rb {
     uint32_t* scene_off;  // device scene offsets of the bodies
     uint32_t num_scenes;
     gsap_contact_params cp;
+    unsigned long long* contacts;  // config model: particle-particle contacts counted by the force kernel
 };
 
 static void rb_free(gsap_rb* h) {
     void* p[] = {h->pos, h->quat, h->lin, h->ang, h->shape, h->pstart, h->npart, h->p_body, h->inv_mass,
                  h->inv_inertia, h->p_pos, h->p_vel, h->p_force, h->p_rel, h->p_mass, h->ref_pos, h->ref_mass, h->shape_inv,
-                 h->pairs, h->entries, h->bmin, h->bmax, h->body_pairs, h->scene_off};
+                 h->pairs, h->entries, h->bmin, h->bmax, h->body_pairs, h->scene_off, h->contacts};
     for (void* q : p)
         if (q) cudaFree(q);
 }
@@ -90,6 +91,7 @@ extern "C" gsap_rb* gsap_rb_create(int32_t max_bodies, int32_t max_particles, in
     A((void**)&h->entries, 4 * Pn + 4);
     A((void**)&h->bmin, 16 * B); A((void**)&h->bmax, 16 * B);
     A((void**)&h->body_pairs, 8ull * h->body_pair_cap);
+    A((void**)&h->contacts, 8);
     if (!ok) {
         set_error(GSAP_ERR_CUDA, "gsap_rb_create: device allocation failed");
         rb_free(h);
@@ -208,6 +210,7 @@ static CfgParams cfg_of(const gsap_rb* h, float dt) {
     p.kt = h->cp.kt;
     p.gy = h->cp.gravity_y;
     for (int a = 0; a < 3; ++a) { p.lo[a] = h->cp.box_lo[a]; p.hi[a] = h->cp.box_hi[a]; }
+    p.contacts = h->contacts;
     return p;
 }
 
@@ -348,6 +351,20 @@ extern "C" gsap_status gsap_rb_get_state(gsap_rb* h, float* pos, float* quat, fl
     return GSAP_OK;
 }
 
+extern "C" gsap_status gsap_rb_set_state(gsap_rb* h, const float* pos, const float* quat, const float* lin,
+                                         const float* ang, void* stream) {
+    if (!h) return set_error(GSAP_ERR_INVALID, "null handle");
+    cudaStream_t st = (cudaStream_t)stream;
+    size_t B = 16ull * h->n_bodies;
+    if (pos) RCK(cudaMemcpyAsync(h->pos, pos, B, cudaMemcpyHostToDevice, st));
+    if (quat) RCK(cudaMemcpyAsync(h->quat, quat, B, cudaMemcpyHostToDevice, st));
+    if (lin) RCK(cudaMemcpyAsync(h->lin, lin, B, cudaMemcpyHostToDevice, st));
+    if (ang) RCK(cudaMemcpyAsync(h->ang, ang, B, cudaMemcpyHostToDevice, st));
+    RCK(cudaStreamSynchronize(st));
+    h->abs_stale = h->cp.model == GSAP_CONTACT_CONFIG;
+    return GSAP_OK;
+}
+
 static void* rb_array(gsap_rb* h, int which, uint64_t* cap) {
     switch (which) {
         case GSAP_RB_PARTICLE_POS: *cap = 16ull * h->max_particles; return h->p_pos;
@@ -384,6 +401,17 @@ extern "C" gsap_status gsap_rb_copy_in(gsap_rb* h, int32_t which, const void* sr
     RCK(cudaStreamSynchronize(st));
     if (which == GSAP_RB_PARTICLE_POS) h->abs_stale = false;
     return GSAP_OK;
+}
+
+extern "C" int gsap_debug_rb_contacts(gsap_rb* h, uint64_t* out, int reset, void* stream) {
+    if (!h || !out) return -1;
+    cudaStream_t st = (cudaStream_t)stream;
+    unsigned long long v = 0;
+    if (cudaMemcpyAsync(&v, h->contacts, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess) return -1;
+    if (reset && cudaMemsetAsync(h->contacts, 0, 8, st) != cudaSuccess) return -1;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+    *out = v;
+    return 0;
 }
 
 // ---------------------------------------------------- PRBWrap replacements

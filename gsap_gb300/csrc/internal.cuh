@@ -3,7 +3,22 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 namespace gsap {
+
+// Launch constants (SM count, occupancy-derived grids) are cached per device
+// ordinal: computed once per device under std::call_once, so concurrent
+// first calls from several host threads are safe and a second device gets
+// its own values.  Ordinals beyond the table are recomputed on every call.
+constexpr int kMaxDevices = 64;
+template <class F>
+int per_device(std::once_flag (&once)[kMaxDevices], int (&val)[kMaxDevices], F compute) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return compute();
+    std::call_once(once[dev], [&] { val[dev] = compute(); });
+    return val[dev];
+}
 
 constexpr int kChunk = 4096;          // objects per PCA / projection work item
 constexpr int kThreads = 256;         // threads per CTA of the streaming kernels
@@ -157,12 +172,18 @@ struct SortGather {
     float4* smin;
     float4* smax;
 };
+// fmode of a sort pass: kSortFlipIn maps float keys to their ordered uint32
+// image as they are loaded (first pass of a float sort), kSortUnflipOut maps
+// them back as they are stored (last pass).
+enum : int { kSortFlipIn = 1, kSortUnflipOut = 2 };
 cudaError_t launch_sort_pass(const BpScratch& s, int pass, int passes, const uint32_t* kin,
                              const uint32_t* vin, uint32_t* kout, uint32_t* vout,
                              const uint32_t* count_ptr, uint64_t cap, uint32_t spin, cudaStream_t st,
-                             const SortGather* gather = nullptr, bool count_next = false);
+                             const SortGather* gather = nullptr, bool count_next = false, int fmode = 0);
+// Counter reset and the digit histograms of a standalone sort (flip != 0:
+// of the float images of the keys).
 cudaError_t launch_sort_prep(const BpScratch& s, const uint32_t* keys, const uint32_t* count_ptr,
-                             uint32_t n, int passes, cudaStream_t st);
+                             uint32_t n, int passes, cudaStream_t st, int flip = 0);
 cudaError_t launch_sweep(const BpScratch& s, const BpArgs& a, const uint32_t* keys,
                          uint2* pairs, uint64_t pair_cap, int count_rows, cudaStream_t st);
 cudaError_t launch_canonical(const BpScratch& s, uint32_t n, const uint2* in_pairs, uint64_t in_cap,

@@ -32,6 +32,7 @@ cudaError_t rb_update_velocity_ref(float4* lin, float4* ang, const float4* quat,
 struct CfgParams {
     float dt, k, eta, kt, gy;
     float lo[3], hi[3];
+    unsigned long long* contacts;  // if set: += particle-particle contacts, counted from both sides
 };
 cudaError_t rb_integrate_cfg(float4* pos, float4* quat, float4* lin, const float4* ang, const CfgParams& p, int n,
                              cudaStream_t st);

@@ -127,49 +127,56 @@ __global__ void __launch_bounds__(256) k_forces_cfg(const float4* __restrict__ p
                                                     const int* pstart, const int* npart, const uint2* body_pairs,
                                                     const uint32_t* rowoff, uint64_t pair_cap, CfgParams p,
                                                     float4* p_force, int np) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= np) return;
-    const int a = p_body[i];
-    const float4 xa = pos[a], ri = p_rel[i], iv = p_vel[i];
-    float3 f = make_float3(0.f, 0.f, 0.f);
-    float3 vw = make_float3(-iv.x, -iv.y, -iv.z);
-    const float xs[3] = {xa.x, xa.y, xa.z}, rs[3] = {ri.x, ri.y, ri.z};
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t ncontact = 0;  // particle-particle contacts of particle i (walls not counted)
+    if (i < np) {
+        const int a = p_body[i];
+        const float4 xa = pos[a], ri = p_rel[i], iv = p_vel[i];
+        float3 f = make_float3(0.f, 0.f, 0.f);
+        float3 vw = make_float3(-iv.x, -iv.y, -iv.z);
+        const float xs[3] = {xa.x, xa.y, xa.z}, rs[3] = {ri.x, ri.y, ri.z};
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        // distance to the walls: (x - lo) + r and (hi - x) - r
-        float pen_lo = ri.w - ((xs[k] - p.lo[k]) + rs[k]);
-        float pen_hi = ri.w - ((p.hi[k] - xs[k]) - rs[k]);
-        if (pen_lo > 0.f) {
-            float3 n = make_float3(k == 0 ? -1.f : 0.f, k == 1 ? -1.f : 0.f, k == 2 ? -1.f : 0.f);
-            contact(p, n, pen_lo, vw, f);
-        }
-        if (pen_hi > 0.f) {
-            float3 n = make_float3(k == 0 ? 1.f : 0.f, k == 1 ? 1.f : 0.f, k == 2 ? 1.f : 0.f);
-            contact(p, n, pen_hi, vw, f);
-        }
-    }
-    uint32_t e0 = rowoff[a], e1 = rowoff[a + 1];
-    if (e1 > pair_cap) e1 = (uint32_t)pair_cap;  // after an overflow (reported) rows stay in storage
-    for (uint32_t e = e0; e < e1; ++e) {
-        int b = (int)__ldg(&body_pairs[e].y);
-        float4 xb = __ldg(pos + b);
-        float bx = xb.x - xa.x, by = xb.y - xa.y, bz = xb.z - xa.z;
-        int s = __ldg(pstart + b), m = __ldg(npart + b);
-        for (int l = 0; l < m; ++l) {
-            float4 rj = __ldg(p_rel + s + l);
-            float dx = bx + (rj.x - ri.x), dy = by + (rj.y - ri.y), dz = bz + (rj.z - ri.z);
-            float d2 = dx * dx + dy * dy + dz * dz;
-            float rr = ri.w + rj.w;
-            if (d2 < rr * rr && d2 > 0.f) {
-                float dist = sqrtf(d2);
-                float inv = 1.f / dist;
-                float4 jv = __ldg(p_vel + s + l);
-                float3 n = make_float3(dx * inv, dy * inv, dz * inv);
-                contact(p, n, rr - dist, make_float3(jv.x - iv.x, jv.y - iv.y, jv.z - iv.z), f);
+        for (int k = 0; k < 3; ++k) {
+            // distance to the walls: (x - lo) + r and (hi - x) - r
+            float pen_lo = ri.w - ((xs[k] - p.lo[k]) + rs[k]);
+            float pen_hi = ri.w - ((p.hi[k] - xs[k]) - rs[k]);
+            if (pen_lo > 0.f) {
+                float3 n = make_float3(k == 0 ? -1.f : 0.f, k == 1 ? -1.f : 0.f, k == 2 ? -1.f : 0.f);
+                contact(p, n, pen_lo, vw, f);
+            }
+            if (pen_hi > 0.f) {
+                float3 n = make_float3(k == 0 ? 1.f : 0.f, k == 1 ? 1.f : 0.f, k == 2 ? 1.f : 0.f);
+                contact(p, n, pen_hi, vw, f);
             }
         }
+        uint32_t e0 = rowoff[a], e1 = rowoff[a + 1];
+        if (e1 > pair_cap) e1 = (uint32_t)pair_cap;  // after an overflow (reported) rows stay in storage
+        for (uint32_t e = e0; e < e1; ++e) {
+            int b = (int)__ldg(&body_pairs[e].y);
+            float4 xb = __ldg(pos + b);
+            float bx = xb.x - xa.x, by = xb.y - xa.y, bz = xb.z - xa.z;
+            int s = __ldg(pstart + b), m = __ldg(npart + b);
+            for (int l = 0; l < m; ++l) {
+                float4 rj = __ldg(p_rel + s + l);
+                float dx = bx + (rj.x - ri.x), dy = by + (rj.y - ri.y), dz = bz + (rj.z - ri.z);
+                float d2 = dx * dx + dy * dy + dz * dz;
+                float rr = ri.w + rj.w;
+                if (d2 < rr * rr && d2 > 0.f) {
+                    float dist = sqrtf(d2);
+                    float inv = 1.f / dist;
+                    float4 jv = __ldg(p_vel + s + l);
+                    float3 n = make_float3(dx * inv, dy * inv, dz * inv);
+                    contact(p, n, rr - dist, make_float3(jv.x - iv.x, jv.y - iv.y, jv.z - iv.z), f);
+                    ++ncontact;
+                }
+            }
+        }
+        p_force[i] = make_float4(f.x, f.y, f.z, 0.f);
     }
-    p_force[i] = make_float4(f.x, f.y, f.z, 0.f);
+    if (p.contacts) {  // one atomic per warp (blocks are whole warps)
+        const uint32_t w = __reduce_add_sync(0xffffffffu, ncontact);
+        if ((threadIdx.x & 31) == 0 && w) atomicAdd(p.contacts, (unsigned long long)w);
+    }
 }
 
 __device__ __forceinline__ void ts_add(float& s, float& c, float x) {

@@ -19,6 +19,13 @@
 
 namespace gsap {
 
+// Order-preserving map of IEEE-754 floats to uint32 (negative values: all
+// bits inverted; non-negative: sign bit set), so that unsigned order of the
+// images is the float order, -0.0 before +0.0 (the floatFlip /
+// floatUnflip pair of sapDetection/radixsort.cu:110-137).
+__device__ __forceinline__ uint32_t flip_f32(uint32_t f) { return f ^ ((f >> 31) ? 0xFFFFFFFFu : 0x80000000u); }
+__device__ __forceinline__ uint32_t unflip_f32(uint32_t f) { return f ^ ((f >> 31) ? 0x80000000u : 0xFFFFFFFFu); }
+
 // Exclusive scan over the 256 threads of a CTA; returns the exclusive value.
 __device__ __forceinline__ uint32_t cta_excl_scan256(uint32_t v, uint32_t* s_w) {
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -43,7 +50,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_onesweep(BpScratch S, const uin
                                                        const uint32_t* __restrict__ vin,
                                                        uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
                                                        const uint32_t* count_ptr, uint32_t cap, int pass,
-                                                       uint32_t spin, SortGather G, int count_next) {
+                                                       uint32_t spin, SortGather G, int count_next, int fmode) {
     constexpr int TILE = kThreads * ITEMS;
     __shared__ uint32_t s_k[TILE];
     __shared__ uint32_t s_next[256];  // histogram of the next pass's digit over this tile
@@ -79,6 +86,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_onesweep(BpScratch S, const uin
             const uint32_t idx = wb0 + k * 32 + lane;
             const bool in = tt < ntiles && idx < n;
             key[k] = in ? __ldcs(kin + idx) : 0u;
+            if (fmode & kSortFlipIn) key[k] = flip_f32(key[k]);
             val[k] = in ? __ldcs(vin + idx) : 0u;
         }
     };
@@ -159,7 +167,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_onesweep(BpScratch S, const uin
                 atomicOr(&S.ctrl->error, kErrInternal);
                 continue;
             }
-            kout[g] = kk;
+            kout[g] = (fmode & kSortUnflipOut) ? unflip_f32(kk) : kk;
             if (vout) vout[g] = vv;
             if (G.smin) {  // last pass of the broadphase: entries in sorted order
                 // The value holds the object index and the entry's owner
@@ -189,12 +197,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_onesweep(BpScratch S, const uin
 
 // Histograms of all passes for a standalone sort.
 template <int PASSES>
-__global__ void __launch_bounds__(kThreads) k_hist(Ctrl* C, const uint32_t* __restrict__ keys, uint32_t n) {
+__global__ void __launch_bounds__(kThreads) k_hist(Ctrl* C, const uint32_t* __restrict__ keys, uint32_t n,
+                                                   int flip) {
     __shared__ uint32_t s_hist[PASSES][256];
     for (uint32_t k = threadIdx.x; k < PASSES * 256; k += kThreads) (&s_hist[0][0])[k] = 0u;
     __syncthreads();
     for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
-        uint32_t key = keys[i];
+        uint32_t key = flip ? flip_f32(keys[i]) : keys[i];
 #pragma unroll
         for (int p = 0; p < PASSES; ++p) atomicAdd(&s_hist[p][(key >> (8 * p)) & 255u], 1u);
     }
@@ -217,33 +226,35 @@ __global__ void k_sort_reset(Ctrl* C, uint32_t n, uint32_t* count_slot) {
 }
 
 cudaError_t launch_sort_prep(const BpScratch& s, const uint32_t* keys, const uint32_t* count_ptr, uint32_t n,
-                             int passes, cudaStream_t st) {
+                             int passes, cudaStream_t st, int flip) {
     k_sort_reset<<<1, 256, 0, st>>>(s.ctrl, n, const_cast<uint32_t*>(count_ptr));
     int grid = sm_count() * 4;
     switch (passes) {
-        case 1: k_hist<1><<<grid, kThreads, 0, st>>>(s.ctrl, keys, n); break;
-        case 2: k_hist<2><<<grid, kThreads, 0, st>>>(s.ctrl, keys, n); break;
-        case 3: k_hist<3><<<grid, kThreads, 0, st>>>(s.ctrl, keys, n); break;
-        default: k_hist<4><<<grid, kThreads, 0, st>>>(s.ctrl, keys, n); break;
+        case 1: k_hist<1><<<grid, kThreads, 0, st>>>(s.ctrl, keys, n, flip); break;
+        case 2: k_hist<2><<<grid, kThreads, 0, st>>>(s.ctrl, keys, n, flip); break;
+        case 3: k_hist<3><<<grid, kThreads, 0, st>>>(s.ctrl, keys, n, flip); break;
+        default: k_hist<4><<<grid, kThreads, 0, st>>>(s.ctrl, keys, n, flip); break;
     }
     return cudaGetLastError();
 }
 
 cudaError_t launch_sort_pass(const BpScratch& s, int pass, int passes, const uint32_t* kin, const uint32_t* vin,
                              uint32_t* kout, uint32_t* vout, const uint32_t* count_ptr, uint64_t cap,
-                             uint32_t spin, cudaStream_t st, const SortGather* gather, bool count_next) {
+                             uint32_t spin, cudaStream_t st, const SortGather* gather, bool count_next, int fmode) {
     SortGather G;
     if (gather) G = *gather;
     else G = SortGather{nullptr, nullptr, nullptr, nullptr};
-    static int grid = 0;
-    if (grid == 0) {
+    static std::once_flag once[kMaxDevices];
+    static int val[kMaxDevices];
+    const int grid = per_device(once, val, [] {
         int per_sm = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_onesweep<kSortItems>, kThreads, 0);
-        grid = sm_count() * (per_sm > 0 ? per_sm : 1);
-    }
+        return sm_count() * (per_sm > 0 ? per_sm : 1);
+    });
     uint32_t c = cap > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)cap;
     const int next = (count_next && pass + 1 < passes) ? 1 : 0;
-    k_onesweep<kSortItems><<<grid, kThreads, 0, st>>>(s, kin, vin, kout, vout, count_ptr, c, pass, spin, G, next);
+    k_onesweep<kSortItems><<<grid, kThreads, 0, st>>>(s, kin, vin, kout, vout, count_ptr, c, pass, spin, G, next,
+                                                      fmode);
     return cudaGetLastError();
 }
 

@@ -142,6 +142,26 @@ class ParticleRigidBody:
                                        C.c_void_p(_stream_ptr(stream))))
         return arrs
 
+    def set_state(self, st: dict, stream=None):
+        """gsap_rb_set_state: body pos / quat / lin_vel / ang_vel (n_bodies x 4
+        float32, any key may be absent) written bit for bit, no
+        normalisation."""
+        arrs = {k: (_host(st[k], np.float32) if st.get(k) is not None else None)
+                for k in ("pos", "quat", "lin_vel", "ang_vel")}
+        for k, a in arrs.items():
+            if a is not None and a.shape != (self.n_bodies, 4):
+                raise ValueError(f"{k} must have shape ({self.n_bodies}, 4)")
+        check(load().gsap_rb_set_state(self._h, *[a.ctypes.data if a is not None else None for a in arrs.values()],
+                                       C.c_void_p(_stream_ptr(stream))))
+
+    def contacts(self, reset: bool = False, stream=None) -> int:
+        """Particle-particle contacts counted by the config-model force
+        kernel since creation or the last reset (both sides counted)."""
+        out = C.c_uint64(0)
+        if load().gsap_debug_rb_contacts(self._h, C.byref(out), int(reset), C.c_void_p(_stream_ptr(stream))) != 0:
+            raise GsapError(3, "contact counter read failed")
+        return int(out.value)
+
     def get_particles(self) -> dict:
         np_ = self.n_particles
         return {"p_pos": self.copy_out(0, (np_, 4)), "p_vel": self.copy_out(1, (np_, 4)),

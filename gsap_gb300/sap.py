@@ -41,18 +41,40 @@ def _dev_ptr(t: torch.Tensor | None, name: str, dtype=None, cols=None) -> int | 
 NOALLOC_SORT_MAX_N = 1 << 20  # GSAP_NOALLOC_SORT_MAX_N
 
 
+def _noalloc_device(keys, vals):
+    """The device the no-alloc sort runs on: the keys' device, which the
+    values must share (the C side checks the pointers against the current
+    device too)."""
+    if not keys.is_cuda:
+        raise ValueError("keys must be a CUDA tensor")
+    if vals is not None:
+        if not vals.is_cuda:
+            raise ValueError("vals must be a CUDA tensor")
+        if vals.device != keys.device:
+            raise ValueError(f"keys are on {keys.device} but vals on {vals.device}")
+        if vals.numel() != keys.numel():
+            raise ValueError("keys and vals must have the same length")
+    return keys.device
+
+
 def radix_sort_noalloc(keys: torch.Tensor, vals: torch.Tensor | None = None, bits: int = 32, stream=None):
     """In-place stable sort like ``Sap.radix_sort`` that allocates no device
     memory and needs no handle: its scratch is a fixed static device array,
     so at most ``NOALLOC_SORT_MAX_N`` keys, and calls that overlap in time
-    race.  The first call on a device does a synchronising set-up."""
+    race.  The first call on a device does a synchronising set-up.  Runs on
+    the keys' device (made current for the call), on `stream` or that
+    device's current stream."""
+    dev = _noalloc_device(keys, vals)
     _dev_ptr(keys, "keys", torch.int32)
     _dev_ptr(vals, "vals", torch.int32)
-    if vals is not None and vals.numel() != keys.numel():
-        raise ValueError("keys and vals must have the same length")
-    check(load().gsap_radix_sort_u32_noalloc(keys.data_ptr(), vals.data_ptr() if vals is not None else None,
-                                             C.c_uint32(keys.numel()), C.c_uint32(bits),
-                                             C.c_void_p(_stream_ptr(stream))))
+    with torch.cuda.device(dev):
+        if stream is None:
+            stream = torch.cuda.current_stream(dev)
+        elif stream.device != dev:
+            raise ValueError(f"stream is on {stream.device}, keys on {dev}")
+        check(load().gsap_radix_sort_u32_noalloc(keys.data_ptr(), vals.data_ptr() if vals is not None else None,
+                                                 C.c_uint32(keys.numel()), C.c_uint32(bits),
+                                                 C.c_void_p(_stream_ptr(stream))))
 
 
 class Sap:
@@ -212,6 +234,19 @@ class Sap:
         _dev_ptr(vals, "vals", torch.int32)
         check(load().gsap_radix_sort_u32(self._h, keys.data_ptr(), vals.data_ptr() if vals is not None else None,
                                          C.c_uint32(keys.numel()), C.c_uint32(bits),
+                                         C.c_void_p(_stream_ptr(stream))))
+
+    def radix_sort_f32(self, keys: torch.Tensor, vals: torch.Tensor | None = None, key_bits: int = 32,
+                       negative_keys: bool = True, stream=None):
+        """RadixSort::sort(float*, uint*, n, keyBits, negativeKeys)
+        (radixsort.h:180-198): in-place stable sort of float32 keys (and
+        int32-stored uint32 values) in float order when negative_keys."""
+        _dev_ptr(keys, "keys", torch.float32)
+        _dev_ptr(vals, "vals", torch.int32)
+        if vals is not None and vals.numel() != keys.numel():
+            raise ValueError("keys and vals must have the same length")
+        check(load().gsap_radix_sort_f32(self._h, keys.data_ptr(), vals.data_ptr() if vals is not None else None,
+                                         C.c_uint32(keys.numel()), C.c_uint32(key_bits), C.c_int(int(negative_keys)),
                                          C.c_void_p(_stream_ptr(stream))))
 
     def stats(self, stream=None) -> dict:

@@ -178,10 +178,31 @@ gsap_status gsap_sap_autotune(gsap_sap* h, const float* d_min, const float* d_ma
 /* Stable LSD radix sort of n (key, value) uint32 pairs on the low `bits`
  * bits with the onesweep kernels of the broadphase (decoupled look-back,
  * 8-bit digits).  Sorts in place; uses the handle's scratch (n must not
- * exceed its entry capacity).  Replaces RadixSort::sort(uint*, uint*, uint,
- * uint) (sapDetection/radixsort.h:180-198). */
+ * exceed its entry capacity); d_vals may be NULL (keys only).  Replaces
+ * RadixSort::sort(uint* keys, uint* values, uint numElements, uint keyBits)
+ * (sapDetection/radixsort.h:151-168).  For keys below 2^bits the order is
+ * the reference's at every n (its paths for n <= 1024 sort on all 32 bits,
+ * radixsort.cu:1396-1412). */
 gsap_status gsap_radix_sort_u32(gsap_sap* h, uint32_t* d_keys, uint32_t* d_vals, uint32_t n,
                                 uint32_t bits, void* stream);
+
+/* Stable LSD radix sort of n float keys and uint32 values (d_vals may be
+ * NULL), in place, on the handle's scratch.  Replaces RadixSort::sort(float*
+ * keys, uint* values, uint numElements, uint keyBits, bool negativeKeys)
+ * (sapDetection/radixsort.h:180-198), the overload of the reference's hot
+ * path (sapDetection/Sap.cpp:235, keyBits 32 and negativeKeys true).
+ *  - negative_keys != 0: ascending float order, -inf < ... < -0.0 < +0.0 <
+ *    ... < +inf (NaNs with the sign bit set come first, the others last),
+ *    through the order-preserving bit map of radixsort.cu:110-137, applied
+ *    as the first pass loads the keys and undone as the last pass stores
+ *    them.  key_bits must be 32: with fewer bits the reference sorts the
+ *    mapped keys on their low bits and, for n > 1024, leaves them mapped
+ *    (radixsort.cu:1414-1478), which this entry point does not reproduce.
+ *  - negative_keys == 0: the keys' bit patterns are sorted as unsigned
+ *    integers on their low key_bits bits (ascending for non-negative
+ *    floats), as the reference does without the map. */
+gsap_status gsap_radix_sort_f32(gsap_sap* h, float* d_keys, uint32_t* d_vals, uint32_t n,
+                                uint32_t key_bits, int negative_keys, void* stream);
 
 /* The same sort for callers that may not allocate device memory when they
  * sort (a pool allocator that owns the device, an allocation-free section
@@ -192,7 +213,10 @@ gsap_status gsap_radix_sort_u32(gsap_sap* h, uint32_t* d_keys, uint32_t* d_vals,
  *     GSAP_ERR_CAPACITY before any work is queued.
  *   - The first call on each device does the set-up (looks up the array,
  *     zeroes its control block and look-back words, synchronises the
- *     device); make it before any stream capture begins.
+ *     device); make it before any stream capture begins.  A set-up that
+ *     failed is retried by the next call.
+ *   - d_keys / d_vals must be device memory of the current device; other
+ *     pointers return GSAP_ERR_INVALID before any work is queued.
  *   - One scratch per device: calls that overlap in time (other streams,
  *     other host threads) race.  Serialise them.
  *   - d_vals may be NULL (keys only).  Synchronises `stream` to read the
@@ -309,6 +333,14 @@ gsap_status gsap_rb_copy_in(gsap_rb* h, int32_t which, const void* h_src, uint64
  * Headless replacement of the GL pose export (ParticleRigidBody.cpp:88-98). */
 gsap_status gsap_rb_get_state(gsap_rb* h, float* h_pos, float* h_quat, float* h_lin_vel,
                               float* h_ang_vel, void* stream);
+
+/* The inverse of gsap_rb_get_state: overwrites the body state of the
+ * n_bodies bodies from host float4 arrays (any may be NULL), bit for bit --
+ * the state half of setRbData (ParticleRigidBody.cpp:78-110) without its
+ * quaternion normalisation, for restarting from a snapshot or re-syncing
+ * to an external trajectory.  Synchronous. */
+gsap_status gsap_rb_set_state(gsap_rb* h, const float* h_pos, const float* h_quat, const float* h_lin_vel,
+                              const float* h_ang_vel, void* stream);
 
 /* Low-level launchers on caller-owned device arrays, replacing the PRBWrap
  * functions (ParticleRigidBodyWrapper.h:15-50) without dim3 arguments

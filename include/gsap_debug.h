@@ -34,6 +34,21 @@ int gsap_debug_stats(struct gsap_sap* h, uint64_t* out8, void* stream);
  * GSAP_ERR_DEVICE_TIMEOUT and leaves the handle and the context usable. */
 int gsap_debug_lookback_timeout(struct gsap_sap* h, uint32_t spin_limit, void* stream);
 
+/* Particle-particle contacts found by the config-model force kernel since
+ * the handle was created or last reset (each contact counted from both
+ * particles, so the contact pairs are *out / 2; walls not counted).  The
+ * kernel adds one warp-aggregated count per warp of every step.  Reads the
+ * counter (synchronizes) and zeroes it when reset != 0.  Returns 0. */
+struct gsap_rb;
+int gsap_debug_rb_contacts(struct gsap_rb* h, uint64_t* out, int reset, void* stream);
+
+/* Graph cache of a broadphase handle: per_shape != 0 sets how many cached
+ * graphs of one shape (sizes, flags, settings) the handle keeps before a
+ * call with new buffers updates one of them in place (default 64);
+ * *out_count (may be NULL) receives the number of cached graphs.
+ * Returns 0. */
+int gsap_debug_graph_cache(struct gsap_sap* h, uint32_t per_shape, uint32_t* out_count);
+
 /* Sizes of internal device structures (control block, scene record, PCA
  * partial, sort tile) for layout checks.  Returns 0. */
 int gsap_debug_sizes(uint32_t* out4);

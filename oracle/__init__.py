@@ -57,7 +57,8 @@ def build(ref: bool = False) -> None:
                     fh.write(platform.machine())
             _BUILT = True
         if ref:
-            subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+            extra = [f"REF={ref}"] if isinstance(ref, str) else []
+            subprocess.run(["make", "-s", "-C", HERE, "ref", *extra], check=True)
 
 
 def _i64(x):
@@ -92,6 +93,12 @@ def lib():
         L.orc_rb_step_ref.restype = C.c_int64
         L.orc_rb_step_cfg_f64.argtypes = [P, P, C.c_int]
         L.orc_rb_step_cfg_f64.restype = C.c_int64
+        L.orc_rb_step_cfg_f64_amb.argtypes = [P, P, C.c_int, C.c_double, P]
+        L.orc_rb_step_cfg_f64_amb.restype = C.c_int64
+        L.orc_body_neighbours.argtypes = [C.c_int, P, P, P, C.c_int, C.c_int, P, P, C.c_int64]
+        L.orc_body_neighbours.restype = C.c_int64
+        L.orc_pairs_batched.argtypes = [P, P, P, C.c_int, C.c_uint32, P, C.c_int64, C.c_int]
+        L.orc_pairs_batched.restype = C.c_int64
         _LIB = L
     return _LIB
 
@@ -155,6 +162,17 @@ def sap_ref(mode, mn, mx=None, threads=0, cap=None):
     L = lib()
     return _run_pairs(lambda a, b, p, c: L.orc_sap_ref(mode, a, b, C.c_uint32(len(mn)), p, c, threads),
                       _ptr(mn), _ptr(mx), cap=cap)
+
+
+def pairs_batched(mn, mx, offsets, bf_max=8192, threads=0, cap=1 << 22):
+    """Sorted (i<j) pairs of every scene of a batch (global ids): the O(n^2)
+    test for scenes of at most bf_max objects, the same predicate on the
+    pairs whose x intervals meet for larger ones."""
+    mn, mx = _f4(mn), _f4(mx)
+    off = np.ascontiguousarray(offsets, np.int64)
+    L = lib()
+    return _run_pairs(lambda a, b, p, c: L.orc_pairs_batched(a, b, _ptr(off), len(off) - 1, C.c_uint32(bf_max), p,
+                                                             c, threads), _ptr(mn), _ptr(mx), cap=cap)
 
 
 def sap_ref_sampled(mode, mn, mx, parts, part, threads=0):
@@ -262,8 +280,11 @@ def rb_step_ref(state: dict, dt, sp_multip, dp_multip, max_lin_vel=0.0, gravity_
     return n
 
 
-def rb_step_cfg_f64(state: dict, params: dict, threads=0):
-    """One config-mode FP64 step on a dict of float64/int32 arrays (in place)."""
+def rb_step_cfg_f64(state: dict, params: dict, threads=0, band=None):
+    """One config-mode FP64 step on a dict of float64/int32 arrays (in place).
+    With `band`, returns an int32 flag per body: 1 where a contact of the
+    step has a penetration depth within +-band of zero (its onset can flip
+    under a rounding of the state of that size)."""
     s = RbStateF64()
     s.n_bodies = len(state["pos"])
     s.n_particles = len(state["p_pos"])
@@ -275,4 +296,25 @@ def rb_step_cfg_f64(state: dict, params: dict, threads=0):
     for a in range(3):
         p.box_lo[a] = params["box_lo"][a]
         p.box_hi[a] = params["box_hi"][a]
-    return lib().orc_rb_step_cfg_f64(C.byref(s), C.byref(p), threads)
+    if band is None:
+        return lib().orc_rb_step_cfg_f64(C.byref(s), C.byref(p), threads)
+    amb = np.zeros(s.n_bodies, np.int32)
+    lib().orc_rb_step_cfg_f64_amb(C.byref(s), C.byref(p), threads, C.c_double(band), _ptr(amb))
+    return amb
+
+
+def body_neighbours(bmin, bmax, scene=None, brute=False, threads=0):
+    """Rows of the FP64 oracle's body pair search: (offsets[nb+1], ids)."""
+    bmin = np.ascontiguousarray(bmin, np.float64)
+    bmax = np.ascontiguousarray(bmax, np.float64)
+    nb = len(bmin)
+    sc = np.ascontiguousarray(scene, np.int32) if scene is not None else None
+    cnt = np.zeros(nb + 1, np.int32)
+    cap = 16 * nb + 16
+    while True:
+        nbr = np.empty(max(cap, 1), np.int32)
+        tot = lib().orc_body_neighbours(nb, _ptr(bmin), _ptr(bmax), _ptr(sc), int(brute), threads, _ptr(cnt),
+                                        _ptr(nbr), _i64(cap))
+        if tot >= 0:
+            return cnt, nbr[:tot].copy()
+        cap = int(cnt[nb])

@@ -146,20 +146,97 @@ void orc_radix_sort_u32(uint32_t* keys, uint32_t* vals, uint32_t n, int bits) {
     free(v2);
 }
 
-/* LSD radix sort of u64 keys (pair keys (i << 32) | j). */
-static void radix_sort_u64(uint64_t* keys, size_t n, int bits) {
+/* Parallel stable LSD radix sort (8-bit digits) of u32 keys with u32
+ * values or of u64 keys, for the CPU baseline: per pass every thread counts
+ * the digits of its contiguous chunk, an exclusive scan in (digit, thread)
+ * order gives each thread its output offsets, and the threads scatter their
+ * chunks in input order, so equal digits keep their order (stable). */
+#define PR_MAXT 256
+static void par_radix_u32(uint32_t* keys, uint32_t* vals, size_t n, int bits, int nt) {
+    if (n < 2 || bits <= 0) return;
+    if (nt > PR_MAXT) nt = PR_MAXT;
+    if (n < 65536) nt = 1;
+    uint32_t* k2 = (uint32_t*)malloc(n * 4);
+    uint32_t* v2 = vals ? (uint32_t*)malloc(n * 4) : NULL;
+    size_t(*cnt)[256] = (size_t(*)[256])malloc((size_t)nt * sizeof(*cnt));
+    uint32_t *ks = keys, *vs = vals, *kd = k2, *vd = v2;
+    for (int shift = 0; shift < bits; shift += 8) {
+#pragma omp parallel num_threads(nt)
+        {
+#ifdef _OPENMP
+            const int t = omp_get_thread_num();
+#else
+            const int t = 0;
+#endif
+            const size_t a = n * (size_t)t / (size_t)nt, b = n * (size_t)(t + 1) / (size_t)nt;
+            size_t* c = cnt[t];
+            memset(c, 0, sizeof(*cnt));
+            for (size_t i = a; i < b; ++i) c[(ks[i] >> shift) & 0xFFu]++;
+#pragma omp barrier
+#pragma omp single
+            {
+                size_t run = 0;
+                for (int d = 0; d < 256; ++d)
+                    for (int u = 0; u < nt; ++u) {
+                        size_t x = cnt[u][d];
+                        cnt[u][d] = run;
+                        run += x;
+                    }
+            }
+            for (size_t i = a; i < b; ++i) {
+                size_t p = c[(ks[i] >> shift) & 0xFFu]++;
+                kd[p] = ks[i];
+                if (vs) vd[p] = vs[i];
+            }
+        }
+        uint32_t* x = ks; ks = kd; kd = x;
+        x = vs; vs = vd; vd = x;
+    }
+    if (ks != keys) {
+        memcpy(keys, ks, n * 4);
+        if (vals) memcpy(vals, vs, n * 4);
+    }
+    free(cnt);
+    free(k2);
+    free(v2);
+}
+
+static void par_radix_u64(uint64_t* keys, size_t n, int bits, int nt) {
     if (n < 2) return;
+    if (nt > PR_MAXT) nt = PR_MAXT;
+    if (n < 65536) nt = 1;
     uint64_t* tmp = (uint64_t*)malloc(n * 8);
+    size_t(*cnt)[256] = (size_t(*)[256])malloc((size_t)nt * sizeof(*cnt));
     uint64_t *s = keys, *d = tmp;
     for (int shift = 0; shift < bits; shift += 8) {
-        size_t cnt[257];
-        memset(cnt, 0, sizeof(cnt));
-        for (size_t i = 0; i < n; ++i) cnt[((s[i] >> shift) & 0xFF) + 1]++;
-        for (int q = 0; q < 256; ++q) cnt[q + 1] += cnt[q];
-        for (size_t i = 0; i < n; ++i) d[cnt[(s[i] >> shift) & 0xFF]++] = s[i];
-        uint64_t* t = s; s = d; d = t;
+#pragma omp parallel num_threads(nt)
+        {
+#ifdef _OPENMP
+            const int t = omp_get_thread_num();
+#else
+            const int t = 0;
+#endif
+            const size_t a = n * (size_t)t / (size_t)nt, b = n * (size_t)(t + 1) / (size_t)nt;
+            size_t* c = cnt[t];
+            memset(c, 0, sizeof(*cnt));
+            for (size_t i = a; i < b; ++i) c[(s[i] >> shift) & 0xFF]++;
+#pragma omp barrier
+#pragma omp single
+            {
+                size_t run = 0;
+                for (int q = 0; q < 256; ++q)
+                    for (int u = 0; u < nt; ++u) {
+                        size_t x = cnt[u][q];
+                        cnt[u][q] = run;
+                        run += x;
+                    }
+            }
+            for (size_t i = a; i < b; ++i) d[c[(s[i] >> shift) & 0xFF]++] = s[i];
+        }
+        uint64_t* x = s; s = d; d = x;
     }
     if (s != keys) memcpy(keys, s, n * 8);
+    free(cnt);
     free(tmp);
 }
 
@@ -185,22 +262,21 @@ static void sweep_group(int mode, const float* mn, const float* mx, int ax,
     uint32_t* keys = (uint32_t*)malloc((size_t)m * 4);
     float* lo = (float*)malloc((size_t)m * 4);
     float* hi = (float*)malloc((size_t)m * 4);
-    for (uint32_t k = 0; k < m; ++k) {
+#pragma omp parallel for schedule(static) num_threads(nt)
+    for (int64_t k = 0; k < (int64_t)m; ++k) {
         uint32_t i = ids[k];
-        float l, h;
+        float l;
         if (mode == 0) {
             l = mn[4 * (size_t)i + ax];
-            h = mx[4 * (size_t)i + ax];
         } else {
             float c = mn[4 * (size_t)i + ax], r = mn[4 * (size_t)i + 3];
             l = c - r;
-            h = c + r;
         }
         keys[k] = orc_float_flip(l);
-        (void)h;
     }
-    orc_radix_sort_u32(keys, ids, m, 32);
-    for (uint32_t k = 0; k < m; ++k) {
+    par_radix_u32(keys, ids, m, 32, nt);
+#pragma omp parallel for schedule(static) num_threads(nt)
+    for (int64_t k = 0; k < (int64_t)m; ++k) {
         uint32_t i = ids[k];
         if (mode == 0) {
             lo[k] = mn[4 * (size_t)i + ax];
@@ -260,7 +336,8 @@ int64_t orc_sap_ref_sampled(int mode, const float* mn, const float* mx, uint32_t
     /* centres: sphere xyz, or AABB midpoints */
     double mean[3] = {0, 0, 0}, var[3] = {0, 0, 0};
     float* cen = (float*)malloc((size_t)n * 12);
-    for (uint32_t i = 0; i < n; ++i)
+#pragma omp parallel for schedule(static) num_threads(nt) reduction(+ : mean[:3])
+    for (int64_t i = 0; i < (int64_t)n; ++i)
         for (int k = 0; k < 3; ++k) {
             float c = mode == 0 ? 0.5f * (mn[4 * (size_t)i + k] + mx[4 * (size_t)i + k])
                                 : mn[4 * (size_t)i + k];
@@ -268,7 +345,8 @@ int64_t orc_sap_ref_sampled(int mode, const float* mn, const float* mx, uint32_t
             mean[k] += c;
         }
     for (int k = 0; k < 3; ++k) mean[k] /= n;
-    for (uint32_t i = 0; i < n; ++i)
+#pragma omp parallel for schedule(static) num_threads(nt) reduction(+ : var[:3])
+    for (int64_t i = 0; i < (int64_t)n; ++i)
         for (int k = 0; k < 3; ++k) {
             double d = cen[3 * (size_t)i + k] - mean[k];
             var[k] += d * d;
@@ -338,15 +416,39 @@ int64_t orc_sap_ref_sampled(int mode, const float* mn, const float* mx, uint32_t
     double t_canon = wall();
     int idbits = 1;
     while (idbits < 32 && ((uint64_t)1 << idbits) < n) ++idbits;
-    radix_sort_u64(all.p, all.n, 32 + ((idbits + 7) / 8) * 8);
+    par_radix_u64(all.p, all.n, 32 + ((idbits + 7) / 8) * 8, nt);
+    /* unique: per-chunk counts of first occurrences, prefix, then write */
     int64_t u = 0;
-    for (size_t k = 0; k < all.n; ++k) {
-        if (k > 0 && all.p[k] == all.p[k - 1]) continue;
-        if (pairs && u < cap) {
-            pairs[2 * u] = (uint32_t)(all.p[k] >> 32);
-            pairs[2 * u + 1] = (uint32_t)all.p[k];
+    {
+        int ct = nt > PR_MAXT ? PR_MAXT : nt;
+        if (all.n < 65536) ct = 1;
+        int64_t cu[PR_MAXT + 1];
+        memset(cu, 0, sizeof(cu));
+#pragma omp parallel num_threads(ct)
+        {
+#ifdef _OPENMP
+            const int t = omp_get_thread_num();
+#else
+            const int t = 0;
+#endif
+            const size_t a = all.n * (size_t)t / (size_t)ct, b = all.n * (size_t)(t + 1) / (size_t)ct;
+            int64_t c = 0;
+            for (size_t k = a; k < b; ++k) c += (k == 0 || all.p[k] != all.p[k - 1]);
+            cu[t + 1] = c;
+#pragma omp barrier
+#pragma omp single
+            for (int q = 0; q < ct; ++q) cu[q + 1] += cu[q];
+            int64_t o = cu[t];
+            for (size_t k = a; k < b; ++k) {
+                if (k > 0 && all.p[k] == all.p[k - 1]) continue;
+                if (pairs && o < cap) {
+                    pairs[2 * o] = (uint32_t)(all.p[k] >> 32);
+                    pairs[2 * o + 1] = (uint32_t)all.p[k];
+                }
+                ++o;
+            }
         }
-        ++u;
+        u = cu[ct];
     }
     t_var += wall() - t_canon;
     for (int q = 0; q < 4; ++q) free(grp[q]);
@@ -393,4 +495,65 @@ int64_t orc_both_directions(const uint32_t* pairs, int64_t np,
     free(cur);
     free(off);
     return ne;
+}
+
+/* ------------------------------------------------------- batched scenes */
+
+static int cmp_u64(const void* a, const void* b) {
+    uint64_t x = *(const uint64_t*)a, y = *(const uint64_t*)b;
+    return (x > y) - (x < y);
+}
+
+/* Pairs of one scene [b, e) of a batch: every i < j of the scene with
+ * Aabb::overlaps (include/aabb.h:47-57), as keys (i << 32) | j in ascending
+ * order.  Scenes of at most bf_max objects test all pairs (the reference's
+ * Demo::cpuBroadphase loop, cudaPhysics/demo.h:404-417); larger ones test
+ * the same predicate on every pair whose x intervals meet, found by a sort
+ * on min x (a pair whose x intervals are disjoint fails the predicate, so
+ * the set is the brute force's). */
+static pvec scene_pairs(const float* mn, const float* mx, uint32_t b, uint32_t e, uint32_t bf_max) {
+    pvec out = {0, 0, 0};
+    const uint32_t m = e - b;
+    if (m < 2) return out;
+    if (m <= bf_max) {
+        for (uint32_t i = b; i < e; ++i)
+            for (uint32_t j = i + 1; j < e; ++j)
+                if (pred_aabb_ix(mn, mx, i, j)) pv_push(&out, ((uint64_t)i << 32) | j);
+        return out;
+    }
+    uint64_t* ord = (uint64_t*)malloc((size_t)m * 8);  /* (flip(min x) << 32) | local index */
+    for (uint32_t k = 0; k < m; ++k) ord[k] = ((uint64_t)orc_float_flip(mn[4 * (size_t)(b + k)]) << 32) | k;
+    qsort(ord, m, 8, cmp_u64);
+    for (uint32_t p = 0; p < m; ++p) {
+        const uint32_t i = b + (uint32_t)ord[p];
+        const float hx = mx[4 * (size_t)i];
+        for (uint32_t q = p + 1; q < m; ++q) {
+            const uint32_t j = b + (uint32_t)ord[q];
+            if (!(mn[4 * (size_t)j] <= hx)) break;
+            if (pred_aabb_ix(mn, mx, i, j)) pv_push(&out, i < j ? ((uint64_t)i << 32) | j : ((uint64_t)j << 32) | i);
+        }
+    }
+    free(ord);
+    qsort(out.p, out.n, 8, cmp_u64);
+    return out;
+}
+
+int64_t orc_pairs_batched(const float* mn, const float* mx, const int64_t* off, int num_scenes, uint32_t bf_max,
+                          uint32_t* pairs, int64_t cap, int threads) {
+    const int nt = nthreads(threads);
+    pvec* per = (pvec*)calloc((size_t)(num_scenes > 0 ? num_scenes : 1), sizeof(pvec));
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+    for (int s = 0; s < num_scenes; ++s) per[s] = scene_pairs(mn, mx, (uint32_t)off[s], (uint32_t)off[s + 1], bf_max);
+    int64_t total = 0;
+    for (int s = 0; s < num_scenes; ++s) {
+        for (size_t k = 0; k < per[s].n; ++k, ++total) {
+            if (pairs && total < cap) {
+                pairs[2 * total] = (uint32_t)(per[s].p[k] >> 32);
+                pairs[2 * total + 1] = (uint32_t)per[s].p[k];
+            }
+        }
+        free(per[s].p);
+    }
+    free(per);
+    return total;
 }

@@ -152,7 +152,25 @@ typedef struct orc_rb_state_d {
 
 /* One config-mode step in double precision.  Returns the number of
  * particle contact pairs (i<j, penetrating or not) examined. */
+/* Batched scenes (object ids [off[s], off[s+1]) per scene): the sorted
+ * (i<j) pairs of Aabb::overlaps within each scene, scenes in order.
+ * Scenes of at most bf_max objects run the O(n^2) loop; larger ones test
+ * the pairs whose x intervals meet (found by a sort on min x). */
+int64_t orc_pairs_batched(const float* mn, const float* mx, const int64_t* off, int num_scenes, uint32_t bf_max,
+                          uint32_t* pairs, int64_t cap, int threads);
+
 int64_t orc_rb_step_cfg_f64(orc_rb_state_d* s, const orc_cfg_params* p, int threads);
+/* The same step, flagging in amb[n_bodies] the bodies with a contact whose
+ * penetration depth is within +-band of zero (see rb.c). */
+int64_t orc_rb_step_cfg_f64_amb(orc_rb_state_d* s, const orc_cfg_params* p, int threads, double band, int* amb);
+
+/* The body pair search of that step: rows of the bodies of the same scene
+ * whose closed AABBs (bmin/bmax: 3 doubles per body) meet, ascending ids;
+ * brute != 0 tests all pairs, else a sort-and-sweep on min x (same set).
+ * cnt: nb + 1 row offsets.  Returns the total, or -1 when cap is short
+ * (cnt[nb] then holds the total). */
+int64_t orc_body_neighbours(int nb, const double* bmin, const double* bmax, const int* scene, int brute,
+                            int threads, int* cnt, int* nbr, int64_t cap);
 
 #ifdef __cplusplus
 }

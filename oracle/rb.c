@@ -260,8 +260,140 @@ static inline void d_contact(const orc_cfg_params* p, const double* n, double pe
     }
 }
 
+/* Body pair search of the FP64 oracle: per body the ids of every other body
+ * of its scene whose closed AABB meets its own (the body broadphase the
+ * GPU step runs), rows in ascending id order.  brute != 0 tests all pairs;
+ * otherwise the bodies of each scene are sorted by min x and each sweeps
+ * forward while the next min x is <= its max x (the same set, O(n log n)).
+ * cnt[nb + 1] receives the row offsets; nbr (capacity cap) the ids.
+ * Returns the total row length, or -1 if cap is too small. */
+typedef struct { double key; int id; } key_id;
+static int cmp_key_id(const void* a, const void* b) {
+    const key_id* x = (const key_id*)a;
+    const key_id* y = (const key_id*)b;
+    if (x->key < y->key) return -1;
+    if (x->key > y->key) return 1;
+    return (x->id > y->id) - (x->id < y->id);
+}
+static int cmp_int(const void* a, const void* b) {
+    int x = *(const int*)a, y = *(const int*)b;
+    return (x > y) - (x < y);
+}
+static inline int box_meets(const double* bmin, const double* bmax, int a, int b) {
+    int ov = 1;
+    for (int k = 0; k < 3; ++k) ov &= bmin[3 * a + k] <= bmax[3 * b + k] && bmin[3 * b + k] <= bmax[3 * a + k];
+    return ov;
+}
+
+int64_t orc_body_neighbours(int nb, const double* bmin, const double* bmax, const int* scene, int brute,
+                            int threads, int* cnt, int* nbr, int64_t cap) {
+    int nt = 1;
+#ifdef _OPENMP
+    nt = threads > 0 ? threads : omp_get_max_threads();
+#else
+    (void)threads;
+#endif
+    for (int a = 0; a <= nb; ++a) cnt[a] = 0;
+    if (brute) {
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nt)
+        for (int a = 0; a < nb; ++a) {
+            int c = 0;
+            for (int b = 0; b < nb; ++b)
+                if (b != a && !(scene && scene[a] != scene[b])) c += box_meets(bmin, bmax, a, b);
+            cnt[a + 1] = c;
+        }
+        for (int a = 0; a < nb; ++a) cnt[a + 1] += cnt[a];
+        if (cnt[nb] > cap) return -1;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nt)
+        for (int a = 0; a < nb; ++a) {
+            int o = cnt[a];
+            for (int b = 0; b < nb; ++b)
+                if (b != a && !(scene && scene[a] != scene[b]) && box_meets(bmin, bmax, a, b)) nbr[o++] = b;
+        }
+        return cnt[nb];
+    }
+    /* group the bodies by scene (stable counting sort), then sort each group by min x */
+    int ns = 1;
+    if (scene)
+        for (int a = 0; a < nb; ++a) if (scene[a] + 1 > ns) ns = scene[a] + 1;
+    int* soff = (int*)calloc((size_t)ns + 1, sizeof(int));
+    for (int a = 0; a < nb; ++a) soff[(scene ? scene[a] : 0) + 1]++;
+    for (int k = 0; k < ns; ++k) soff[k + 1] += soff[k];
+    int* fill = (int*)malloc((size_t)ns * sizeof(int));
+    for (int k = 0; k < ns; ++k) fill[k] = soff[k];
+    key_id* ord = (key_id*)malloc((size_t)(nb > 0 ? nb : 1) * sizeof(key_id));
+    for (int a = 0; a < nb; ++a) {
+        const int g = scene ? scene[a] : 0;
+        ord[fill[g]].key = bmin[3 * a];
+        ord[fill[g]].id = a;
+        fill[g]++;
+    }
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+    for (int k = 0; k < ns; ++k) qsort(ord + soff[k], (size_t)(soff[k + 1] - soff[k]), sizeof(key_id), cmp_key_id);
+    /* forward sweep: count per body, then fill */
+    int* grp_end = (int*)malloc((size_t)(nb > 0 ? nb : 1) * sizeof(int));
+    for (int k = 0; k < ns; ++k)
+        for (int q = soff[k]; q < soff[k + 1]; ++q) grp_end[q] = soff[k + 1];
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nt)
+    for (int q = 0; q < nb; ++q) {
+        const int a = ord[q].id;
+        const double hx = bmax[3 * a];
+        int c = 0;
+        for (int r = q + 1; r < grp_end[q] && ord[r].key <= hx; ++r) {
+            const int b = ord[r].id;
+            if (box_meets(bmin, bmax, a, b)) {
+#pragma omp atomic
+                cnt[b + 1]++;
+                ++c;
+            }
+        }
+#pragma omp atomic
+        cnt[a + 1] += c;
+    }
+    for (int a = 0; a < nb; ++a) cnt[a + 1] += cnt[a];
+    int64_t total = cnt[nb];
+    if (total <= cap) {
+        int* cur = (int*)malloc((size_t)(nb > 0 ? nb : 1) * sizeof(int));
+        for (int a = 0; a < nb; ++a) cur[a] = cnt[a];
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nt)
+        for (int q = 0; q < nb; ++q) {
+            const int a = ord[q].id;
+            const double hx = bmax[3 * a];
+            for (int r = q + 1; r < grp_end[q] && ord[r].key <= hx; ++r) {
+                const int b = ord[r].id;
+                if (box_meets(bmin, bmax, a, b)) {
+                    int sa, sb;
+#pragma omp atomic capture
+                    sa = cur[a]++;
+#pragma omp atomic capture
+                    sb = cur[b]++;
+                    nbr[sa] = b;
+                    nbr[sb] = a;
+                }
+            }
+        }
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nt)
+        for (int a = 0; a < nb; ++a) qsort(nbr + cnt[a], (size_t)(cnt[a + 1] - cnt[a]), sizeof(int), cmp_int);
+        free(cur);
+    }
+    free(grp_end);
+    free(ord);
+    free(fill);
+    free(soff);
+    return total <= cap ? total : -1;
+}
+
 int64_t orc_rb_step_cfg_f64(orc_rb_state_d* s, const orc_cfg_params* p, int threads) {
-    const int nb = s->n_bodies, np = s->n_particles;
+    return orc_rb_step_cfg_f64_amb(s, p, threads, 0.0, NULL);
+}
+
+/* The same step; with amb != NULL also flags (amb[b] = 1, else 0) every body
+ * with a contact whose penetration depth lies within +-band of zero: a
+ * particle pair or a wall where a rounding of the state by about band can
+ * switch the contact, and with it the damping force, on or off.  Body boxes
+ * are widened by band for the pair search so that no such pair is missed. */
+int64_t orc_rb_step_cfg_f64_amb(orc_rb_state_d* s, const orc_cfg_params* p, int threads, double band, int* amb) {
+    const int nb = s->n_bodies;
     const double dt = p->dt;
     int nt = 1;
 #ifdef _OPENMP
@@ -270,6 +402,7 @@ int64_t orc_rb_step_cfg_f64(orc_rb_state_d* s, const orc_cfg_params* p, int thre
     (void)threads;
 #endif
     /* integrate: v += g dt; q += 0.5 dt (w,0) q, normalised; x += v dt */
+#pragma omp parallel for schedule(static) num_threads(nt)
     for (int b = 0; b < nb; ++b) {
         double* v = s->lin_vel + 4 * b;
         v[1] += p->gravity_y * dt;
@@ -283,8 +416,9 @@ int64_t orc_rb_step_cfg_f64(orc_rb_state_d* s, const orc_cfg_params* p, int thre
         for (int a = 0; a < 3; ++a) s->pos[4 * b + a] += v[a] * dt;
     }
     /* place particles */
-    double* bmin = (double*)malloc((size_t)nb * 3 * sizeof(double));
-    double* bmax = (double*)malloc((size_t)nb * 3 * sizeof(double));
+    double* bmin = (double*)malloc((size_t)(nb > 0 ? nb : 1) * 3 * sizeof(double));
+    double* bmax = (double*)malloc((size_t)(nb > 0 ? nb : 1) * 3 * sizeof(double));
+#pragma omp parallel for schedule(static) num_threads(nt)
     for (int b = 0; b < nb; ++b) {
         double R[9];
         d_qmat(s->quat + 4 * b, R);
@@ -306,34 +440,21 @@ int64_t orc_rb_step_cfg_f64(orc_rb_state_d* s, const orc_cfg_params* p, int thre
             pv[3] = 0;
         }
     }
-    /* body-AABB brute force (closed test) -> per-body neighbour rows */
-    int* cnt = (int*)calloc((size_t)nb + 1, sizeof(int));
-#pragma omp parallel for schedule(dynamic, 16) num_threads(nt)
-    for (int a = 0; a < nb; ++a) {
-        int c = 0;
+    if (amb) {
         for (int b = 0; b < nb; ++b) {
-            if (b == a) continue;
-            if (s->scene && s->scene[a] != s->scene[b]) continue;
-            int ov = 1;
-            for (int k = 0; k < 3; ++k)
-                ov &= bmin[3 * a + k] <= bmax[3 * b + k] && bmin[3 * b + k] <= bmax[3 * a + k];
-            c += ov;
+            amb[b] = 0;
+            for (int a = 0; a < 3; ++a) { bmin[3 * b + a] -= band; bmax[3 * b + a] += band; }
         }
-        cnt[a + 1] = c;
     }
-    for (int a = 0; a < nb; ++a) cnt[a + 1] += cnt[a];
-    int* nbr = (int*)malloc((size_t)(cnt[nb] > 0 ? cnt[nb] : 1) * sizeof(int));
-#pragma omp parallel for schedule(dynamic, 16) num_threads(nt)
-    for (int a = 0; a < nb; ++a) {
-        int o = cnt[a];
-        for (int b = 0; b < nb; ++b) {
-            if (b == a) continue;
-            if (s->scene && s->scene[a] != s->scene[b]) continue;
-            int ov = 1;
-            for (int k = 0; k < 3; ++k)
-                ov &= bmin[3 * a + k] <= bmax[3 * b + k] && bmin[3 * b + k] <= bmax[3 * a + k];
-            if (ov) nbr[o++] = b;
-        }
+    /* body-AABB pairs (closed test) -> per-body neighbour rows in id order */
+    int* cnt = (int*)malloc(((size_t)nb + 1) * sizeof(int));
+    int64_t cap = 64 * (int64_t)nb + 1024;
+    int* nbr = (int*)malloc((size_t)cap * sizeof(int));
+    if (orc_body_neighbours(nb, bmin, bmax, s->scene, 0, threads, cnt, nbr, cap) < 0) {
+        cap = cnt[nb];
+        free(nbr);
+        nbr = (int*)malloc((size_t)(cap > 0 ? cap : 1) * sizeof(int));
+        orc_body_neighbours(nb, bmin, bmax, s->scene, 0, threads, cnt, nbr, cap);
     }
     int64_t examined = 0;
     /* particle forces: walls, then neighbour bodies in id order */
@@ -347,6 +468,7 @@ int64_t orc_rb_step_cfg_f64(orc_rb_state_d* s, const orc_cfg_params* p, int thre
             for (int ax = 0; ax < 3; ++ax) {
                 double pen_lo = ip[3] - (ip[ax] - p->box_lo[ax]);
                 double pen_hi = ip[3] - (p->box_hi[ax] - ip[ax]);
+                if (amb && (fabs(pen_lo) < band || fabs(pen_hi) < band)) amb[a] = 1;
                 double vrel[3] = {-iv[0], -iv[1], -iv[2]};
                 if (pen_lo > 0) {
                     double n[3] = {0, 0, 0};
@@ -368,6 +490,7 @@ int64_t orc_rb_step_cfg_f64(orc_rb_state_d* s, const orc_cfg_params* p, int thre
                     double d[3] = {jp[0] - ip[0], jp[1] - ip[1], jp[2] - ip[2]};
                     double dist = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
                     double pen = ip[3] + jp[3] - dist;
+                    if (amb && fabs(pen) < band) amb[a] = 1;
                     ++examined;
                     if (pen > 0 && dist > 0) {
                         double n[3] = {d[0] / dist, d[1] / dist, d[2] / dist};
@@ -381,6 +504,7 @@ int64_t orc_rb_step_cfg_f64(orc_rb_state_d* s, const orc_cfg_params* p, int thre
         }
     }
     /* per-body reduction and velocity update: omega += I_w^-1 tau dt */
+#pragma omp parallel for schedule(static) num_threads(nt)
     for (int b = 0; b < nb; ++b) {
         double R[9];
         d_qmat(s->quat + 4 * b, R);

@@ -145,6 +145,64 @@ def test_batched_matches_per_scene(cuda, oracle_lib):
     assert np.array_equal(got, want)
 
 
+def test_graph_mode_with_new_buffers_every_call(cuda, oracle_lib):
+    """Graph mode where every call brings new input and output buffers:
+    once the handle keeps its quota of graphs for the shape (set to 2 here),
+    new buffers update a cached graph in place instead of adding one; every
+    call's pair list is exact."""
+    import ctypes as C
+
+    import torch
+    from gsap_gb300 import Sap, _lib, scenes
+    L = _lib.load()
+    sap = Sap(16384)
+    assert L.gsap_debug_graph_cache(sap.handle, 2, None) == 0
+    n = 16384
+    big_mn = torch.empty((n + 64, 4), dtype=torch.float32, device=cuda)
+    big_mx = torch.empty_like(big_mn)
+    out = torch.empty((16 * n + 64, 2), dtype=torch.int32, device=cuda)
+    for k in range(7):
+        mn, mx = scenes.aabb_uniform(n, k)
+        a = 3 * k  # a new window of the buffers every call: new pointers, same shape
+        big_mn[a:a + n] = to_dev(mn, cuda)
+        big_mx[a:a + n] = to_dev(mx, cuda)
+        got = sap.broadphase(big_mn[a:a + n], big_mx[a:a + n], pairs=out[5 * k:5 * k + 16 * n], sorted=True,
+                            graph=True)
+        assert np.array_equal(got.cpu().numpy().astype(np.uint32), oracle_lib.bf_aabb(mn, mx)), k
+        cnt = C.c_uint32(0)
+        L.gsap_debug_graph_cache(sap.handle, 0, C.byref(cnt))
+        assert cnt.value == min(k + 1, 2)
+
+
+def test_batched_4096_scenes_full_size(cuda, oracle_lib):
+    """The batched workload at its own size: 4096 scenes of 64 to 65,536
+    AABBs (38.6M objects) in one batched call.  The sorted (i<j) list equals
+    the oracle scene by scene (the O(n^2) test for every scene of at most
+    8,192 objects, the same predicate on the pairs whose x intervals meet
+    for larger ones), and sampled scenes run alone through the plain
+    pipeline give the batch's rows for them."""
+    import torch
+    from gsap_gb300 import Sap, scenes
+    mn, mx, off = scenes.batched_aabb(S=4096, seed=7)
+    n = len(mn)
+    dmn, dmx = to_dev(mn, cuda), to_dev(mx, cuda)
+    doff = torch.from_numpy(off.astype(np.int32)).to(cuda)
+    bsap = Sap(n, max_scenes=4096, pair_factor=2)
+    got = bsap.broadphase_batched(dmn, dmx, doff).cpu().numpy().astype(np.uint32)
+    bsap.close()
+    want = oracle_lib.pairs_batched(mn, mx, off, bf_max=8192)
+    assert len(got) == len(want) and np.array_equal(got, want)
+    sizes = off[1:] - off[:-1]
+    sample = [int(np.argmax(sizes)), int(np.argmin(sizes))] + list(range(0, 4096, 512))
+    psap = Sap(int(sizes.max()))
+    lo = np.searchsorted(got[:, 0], off[:-1])
+    hi = np.searchsorted(got[:, 0], off[1:])
+    for s in sample:
+        a, b = int(off[s]), int(off[s + 1])
+        alone = run_bp(psap, mn[a:b], mx[a:b], cuda).astype(np.int64) + a
+        assert np.array_equal(alone.astype(np.uint32), got[lo[s]:hi[s]]), s
+
+
 @pytest.mark.parametrize("axis_mode", [0, 1])
 def test_gauss_1m_against_cpu_sap(cuda, oracle_lib, axis_mode):
     """Full-size 1,048,576-AABB case: equal to the CPU restatement of the
