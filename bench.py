@@ -460,12 +460,15 @@ def run_ours(args, world, rank, local):
     return line
 
 
-def run_extras(args, dev, stream):
-    """Batched scenes vs the plain per-scene pipeline, and the rigid-body step."""
+def _extra_small(args, dev, stream, out):
     import torch
 
     from gsap_gb300 import CONTACT_CONFIG, ParticleRigidBody, Sap, scenes
-    out = {}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    peak, _ = peaks()
+    dt = 1.0 / 600.0
+    cfgp = dict(k=2e4, eta=50.0, kt=0.1, gravity_y=-9.81, box_lo=(0.0, 0.0, 0.0), box_hi=(200.0, 200.0, 200.0))
+    gstream = torch.cuda.Stream()
     # --- small case: 16,384 AABBs, centres U[0,100]^3, half-extents U[0.1,0.5];
     # the reference's own CPU path for it is the O(n^2) brute force
     smn, smx = scenes.aabb_uniform(16384, 0)
@@ -496,14 +499,29 @@ def run_extras(args, dev, stream):
                                              and int(scnt.item()) == len(bf))
     out["small_16k"] = small
     del ssap, spairs
+
+
+def _extra_demo(args, dev, stream, out):
+    import torch
+
+    from gsap_gb300 import CONTACT_CONFIG, ParticleRigidBody, Sap, scenes
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    peak, _ = peaks()
+    dt = 1.0 / 600.0
+    cfgp = dict(k=2e4, eta=50.0, kt=0.1, gravity_y=-9.81, box_lo=(0.0, 0.0, 0.0), box_hi=(200.0, 200.0, 200.0))
+    gstream = torch.cuda.Stream()
     # --- the reference's own call: Sap::collision on the particles of the
     # headless demo scene (4096 hexagon bodies x 6 particles = 24,576 spheres,
     # demoParticles.h:403, :898-903), both-direction list + pairEntries
     from gsap_gb300 import demo
+    # the scene after 300 demo steps (the bodies have fallen and pile up, so
+    # the particles touch as in the demo's later frames)
     dsc = demo.demo_scene(4096, n_row=16, seed=0)
-    dprb = ParticleRigidBody(4096, dsc["n_particles"], 16)
-    dprb.load_scene(dsc)
-    dprb.update_particle_data()
+    dd = demo.Demo(dsc)
+    dd.run(300, stream=stream)
+    torch.cuda.synchronize()
+    dd.sap.check()
+    dprb = dd.system
     dsph = torch.from_numpy(dprb.get_particles()["p_pos"]).to(dev)
     nsp = dsph.shape[0]
     csap = Sap(nsp, mode=1)
@@ -529,7 +547,18 @@ def run_extras(args, dev, stream):
                                             np.array_equal(cpairs[:npc].cpu().numpy(), wp) and
                                             np.array_equal(cent[:nec].cpu().numpy(), we))
     out["demo_collision_24k"] = coll
-    del dprb, csap, cpairs, cent
+    del dprb, dd, csap, cpairs, cent
+
+
+def _extra_large(args, dev, stream, out):
+    import torch
+
+    from gsap_gb300 import CONTACT_CONFIG, ParticleRigidBody, Sap, scenes
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    peak, _ = peaks()
+    dt = 1.0 / 600.0
+    cfgp = dict(k=2e4, eta=50.0, kt=0.1, gravity_y=-9.81, box_lo=(0.0, 0.0, 0.0), box_hi=(200.0, 200.0, 200.0))
+    gstream = torch.cuda.Stream()
     # --- large case: 16,777,216 AABBs at the 1M workload's object density
     # (spread scaled by 16^(1/3)); one input set of 512 MiB, larger than L2
     nl = 1 << 24
@@ -556,6 +585,17 @@ def run_extras(args, dev, stream):
                         "sample": "one seeded 16,777,216-AABB scene, 10 graph calls after the autotuner"}
     lsap.close()
     del lsap, lpairs, dlmn, dlmx
+
+
+def _extra_batched(args, dev, stream, out):
+    import torch
+
+    from gsap_gb300 import CONTACT_CONFIG, ParticleRigidBody, Sap, scenes
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    peak, _ = peaks()
+    dt = 1.0 / 600.0
+    cfgp = dict(k=2e4, eta=50.0, kt=0.1, gravity_y=-9.81, box_lo=(0.0, 0.0, 0.0), box_hi=(200.0, 200.0, 200.0))
+    gstream = torch.cuda.Stream()
     # --- batched broadphase: 4096 scenes, sizes log-uniform in [64, 65536]
     S = args.scenes
     mn, mx, off = scenes.batched_aabb(S=S, seed=7)
@@ -570,7 +610,9 @@ def run_extras(args, dev, stream):
 
     from gsap_gb300 import _lib
     L = _lib.load()
-    btuned = bsap.autotune(dmn, dmx, offsets=doff, pairs=pairs, sorted=True, graph=True, reps=3, stream=stream)
+    btuned = (dict(sort_bits=32, cell_factor=2.0, autotuned=False) if args.no_tune else
+              dict(bsap.autotune(dmn, dmx, offsets=doff, pairs=pairs, sorted=True, graph=True, reps=3, stream=stream),
+                   autotuned=True))
 
     def batched_call():
         st = L.gsap_broadphase_batched(bsap.handle, dmn.data_ptr(), dmx.data_ptr(), doff.data_ptr(), S, n,
@@ -622,13 +664,23 @@ def run_extras(args, dev, stream):
                       "speedup_vs_plain": round(plain_ms / batched_ms, 2),
                       "achieved_gbs": round(bbytes / (batched_ms / 1e3) / 1e9, 1),
                       "frac": round(bbytes / (batched_ms / 1e3) / 1e9 / peak, 4),
-                      "settings": dict(btuned, autotuned=True),
+                      "settings": btuned,
                       "equal_to_reference": equal,
                       "reference": "oracle per scene: O(n^2) Aabb::overlaps for scenes <= 8192 objects, the same "
                                    "predicate on x-overlapping pairs above (untimed check of the timed output)"}
     del bsap, psap, pairs, dmn, dmx
     torch.cuda.empty_cache()
 
+
+def _extra_rigid(args, dev, stream, out):
+    import torch
+
+    from gsap_gb300 import CONTACT_CONFIG, ParticleRigidBody, Sap, scenes
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    peak, _ = peaks()
+    dt = 1.0 / 600.0
+    cfgp = dict(k=2e4, eta=50.0, kt=0.1, gravity_y=-9.81, box_lo=(0.0, 0.0, 0.0), box_hi=(200.0, 200.0, 200.0))
+    gstream = torch.cuda.Stream()
     # --- rigid body: 65,536 cubes of 2x2x2 particles in a 200^3 box, 1000 steps
     dt = 1.0 / 600.0
     nb = args.bodies
@@ -688,7 +740,7 @@ def run_extras(args, dev, stream):
     torch.cuda.synchronize()
     rsap.check()
     prb.contacts(reset=True)
-    steps = 1000
+    steps = args.rb_steps
     e0.record(stream)
     for _ in range(steps):
         graph.replay()
@@ -715,6 +767,16 @@ def run_extras(args, dev, stream):
     del prb, rsap, graph
     torch.cuda.empty_cache()
 
+
+def _extra_rigid_batched(args, dev, stream, out):
+    import torch
+
+    from gsap_gb300 import CONTACT_CONFIG, ParticleRigidBody, Sap, scenes
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    peak, _ = peaks()
+    dt = 1.0 / 600.0
+    cfgp = dict(k=2e4, eta=50.0, kt=0.1, gravity_y=-9.81, box_lo=(0.0, 0.0, 0.0), box_hi=(200.0, 200.0, 200.0))
+    gstream = torch.cuda.Stream()
     # --- batched dynamics: 1024 scenes of 256..8192 bodies (cubes, rods, L shapes) in a 100^3 box
     ms_ = scenes.mixed_scenes(S=args.rb_scenes, seed=4)
     bo = ms_["body_offsets"]
@@ -751,7 +813,7 @@ def run_extras(args, dev, stream):
     torch.cuda.synchronize()
     bsap2.check()
     bprb.contacts(reset=True)
-    bsteps = 100
+    bsteps = args.rb_batched_steps
     e0.record(stream)
     for _ in range(bsteps):
         bgraph.replay()
@@ -789,6 +851,24 @@ def run_extras(args, dev, stream):
                 "plain_sample": f"first {nplain} scenes, one system each, stepped in turn (eager launches)",
                 "speedup_vs_plain": round((args.rb_scenes / b_ms) / (nplain / p_ms), 2)})
     out["rigid_batched"] = rbb
+
+
+
+EXTRAS = ("small", "demo", "large", "batched", "rigid", "rigid_batched")
+
+
+def run_extras(args, dev, stream, which=EXTRAS):
+    """The other workloads, each measured on its own: the 16,384-box case
+    against the O(n^2) brute force, Sap::collision on the demo's 24,576
+    spheres, a 16,777,216-box scene, 4096 batched scenes against the plain
+    per-scene pipeline, the 65,536-cube rigid-body step and the batched
+    dynamics."""
+    import torch
+    out = {}
+    for name in which:
+        globals()[f"_extra_{name}"](args, dev, stream, out)
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
     return out
 
 
@@ -861,6 +941,8 @@ def main():
     ap.add_argument("--scenes", type=int, default=4096)
     ap.add_argument("--bodies", type=int, default=65536)
     ap.add_argument("--rb-scenes", type=int, default=1024)
+    ap.add_argument("--rb-steps", type=int, default=1000, help="timed steps of the 65,536-cube rigid-body step")
+    ap.add_argument("--rb-batched-steps", type=int, default=100, help="timed steps of the batched dynamics")
     ap.add_argument("--rb-check-steps", type=int, default=100,
                     help="steps of the FP64 trajectory checks of the rigid-body extras")
     ap.add_argument("--rb-check-scenes", type=int, default=128,
@@ -873,10 +955,25 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (defaults: 32 bits, cell factor 2.0)")
     ap.add_argument("--jitter-sets", type=int, default=N_JITTER,
                     help="distinct jittered inputs cycled by the timed calls (64 = the workload)")
+    ap.add_argument("--only", default=None,
+                    help="run only these extras (comma-separated: " + ",".join(EXTRAS) + ") and print them, "
+                         "for profiling one workload")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     world, rank, local = dist_setup()
+    if args.only:
+        import torch
+        import gsap_gb300
+        torch.cuda.set_device(local)
+        gsap_gb300.load()
+        which = [w for w in args.only.split(",") if w]
+        bad = [w for w in which if w not in EXTRAS]
+        if bad:
+            raise SystemExit(f"unknown extras {bad}; choose from {EXTRAS}")
+        out = run_extras(args, torch.device("cuda", local), torch.cuda.current_stream(), which)
+        print(json.dumps({"extras": out}), flush=True)
+        return
     if args.impl == "reference":
         if rank != 0:
             return

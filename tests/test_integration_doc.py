@@ -21,11 +21,19 @@ def test_integration_shims_compile(tmp_path):
     if not gxx or not os.path.exists(os.path.join(cuda_inc, "vector_types.h")):
         pytest.skip("needs g++ and the CUDA headers (float4 / int2 of the reference's code)")
     blocks = cpp_blocks()
-    assert len(blocks) >= 3
-    shim, demo_step, fused_step = blocks[0], blocks[1], blocks[2]
+    assert len(blocks) >= 4
+
+    def pick(marker):
+        found = [b for b in blocks if marker in b]
+        assert len(found) == 1, marker
+        return found[0]
+
+    shim, demo_step, fused_step = pick("class Sap"), pick("gsap_rb_integrate(rb"), pick("gsap_rb_step(")
+    standalone = [b for b in blocks if b not in (shim, demo_step, fused_step)]
     src = "\n".join([
         "#include <vector_types.h>",
         shim,
+        *standalone,
         "void demo_step(gsap_rb* rb, Sap& sap, float dt) {",
         demo_step,
         "}",
