@@ -255,16 +255,17 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
 
 cudaError_t launch_sweep(const BpScratch& s, const BpArgs& a, const uint32_t* keys,
                          uint2* pairs, uint64_t pair_cap, int count_rows, cudaStream_t st) {
-    static int grid[2] = {0, 0};
-    int m = a.mode == 1 ? 1 : 0;
-    if (grid[m] == 0) {
+    static std::once_flag once[2][kMaxDevices];
+    static int val[2][kMaxDevices];
+    const int m = a.mode == 1 ? 1 : 0;
+    const int grid = per_device(once[m], val[m], [m] {
         int per_sm = 0;
         if (m == 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep<0>, kThreads, 0);
         else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep<1>, kThreads, 0);
-        grid[m] = sm_count() * (per_sm > 0 ? per_sm : 1);
-    }
-    if (m == 0) k_sweep<0><<<grid[m], kThreads, 0, st>>>(s, a, keys, pairs, pair_cap, count_rows);
-    else k_sweep<1><<<grid[m], kThreads, 0, st>>>(s, a, keys, pairs, pair_cap, count_rows);
+        return sm_count() * (per_sm > 0 ? per_sm : 1);
+    });
+    if (m == 0) k_sweep<0><<<grid, kThreads, 0, st>>>(s, a, keys, pairs, pair_cap, count_rows);
+    else k_sweep<1><<<grid, kThreads, 0, st>>>(s, a, keys, pairs, pair_cap, count_rows);
     return cudaGetLastError();
 }
 
