@@ -199,15 +199,19 @@ def run_ours(args, world, rank, local):
     n = args.n
     host_sets, R = make_inputs(rank, n, args.jitter_sets)
     dsets = [(torch.from_numpy(mn).to(dev), torch.from_numpy(mx).to(dev)) for mn, mx in host_sets]
-    fixed = args.cell_factor is not None or args.sort_bits is not None or args.no_tune
-    sap = Sap(n, cell_factor=args.cell_factor or 2.0, sort_bits=args.sort_bits or 32)
+    fixed = (args.cell_factor is not None or args.sort_bits is not None or args.sort is not None
+             or args.no_tune)
+    sort_mode = {"radix": 0, "bucket": 1}[args.sort or "radix"]
+    sap = Sap(n, cell_factor=args.cell_factor or 2.0, sort_bits=args.sort_bits or 32, sort_mode=sort_mode)
     cap = 16 * n
     pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
     d_count = torch.zeros(1, dtype=torch.int64, device=dev)
     stream = torch.cuda.current_stream()
-    # autotuner (set-up, untimed): key width and cell factor for this input
+    # autotuner (set-up, untimed): sort, key width and cell factor for this input
     tuned = None if fixed else sap.autotune(*dsets[0], pairs=pairs, sorted=True, graph=True, reps=10, stream=stream)
     passes = (tuned["sort_bits"] if tuned else (args.sort_bits or 32)) // 8
+    if tuned:
+        sort_mode = 0 if tuned["sort"] == "radix" else 1
 
     def call(k, sorted_=True, graph=True):
         mn, mx = dsets[k % len(dsets)]
@@ -409,8 +413,10 @@ def run_ours(args, world, rank, local):
     if not args.no_extras:
         extras = run_extras(args, dev, stream)
 
-    # pca + finish, project, one per radix pass, sweep, row sums + row scan, scatter, rank, long rows
-    launches_per_call = 9 + passes
+    # pca + finish, project, the sort (bucket: count sums, offsets, scatter,
+    # local sort; radix: one per pass), sweep, row sums + row scan, scatter,
+    # rank, long rows
+    launches_per_call = 9 + (4 if sort_mode == 1 else passes)
     clocks = clk.summary()
     line = {
         "metric": "1M-AABB PCA sweep-and-prune broadphase throughput (sorted i<j pair set)",
@@ -420,7 +426,8 @@ def run_ours(args, world, rank, local):
         "config": workload_config(args, world),
         "pairs_per_call": P0,
         "settings": dict(tuned, autotuned=True) if tuned else
-        {"sort_bits": args.sort_bits or 32, "cell_factor": args.cell_factor or 2.0, "autotuned": False},
+        {"sort_bits": args.sort_bits or 32, "cell_factor": args.cell_factor or 2.0, "sort": args.sort or "radix",
+         "autotuned": False},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": f"stage:{dom}",
                      "peak_kind": peak_kind,
@@ -436,7 +443,8 @@ def run_ours(args, world, rank, local):
         "stage_ms": {k: round(v, 4) for k, v in st_ms.items()},
         "sweep_stats": {"entries": stats["entries"], "tests": stats["tests"], "buckets": stats["buckets"],
                         "qbits": stats["qbits"], "warp_iters": stats["iters"],
-                        "lane_efficiency": round(stats["tests"] / max(1, 32 * stats["iters"]), 3)},
+                        "lane_efficiency": round(stats["tests"] / max(1, 32 * stats["iters"]), 3),
+                        "tests_per_pair": round(stats["tests"] / max(1, P0), 2)},
         "unsorted_ms_per_step": round(unsorted_ms, 4),
         "new_buffers_every_call": {"ms_per_step": round(fresh_ms, 4), "host_ms_per_call": round(host_s / KF * 1e3, 4),
                                    "calls": KF, "cached_ms_per_step": round(ms, 4),
@@ -610,7 +618,7 @@ def _extra_batched(args, dev, stream, out):
 
     from gsap_gb300 import _lib
     L = _lib.load()
-    btuned = (dict(sort_bits=32, cell_factor=2.0, autotuned=False) if args.no_tune else
+    btuned = (dict(sort_bits=32, cell_factor=2.0, sort="radix", autotuned=False) if args.no_tune else
               dict(bsap.autotune(dmn, dmx, offsets=doff, pairs=pairs, sorted=True, graph=True, reps=3, stream=stream),
                    autotuned=True))
 
@@ -702,6 +710,8 @@ def _extra_rigid(args, dev, stream, out):
         t0 = time.perf_counter()
         e = fp64_errors(prb, rsap, sc, dict(cfgp, dt=dt), steps=args.rb_check_steps, stream=stream)
         rb["fp64_error"] = {"steps": e["steps"], "per_step_max": e["per_step_max"],
+                            "per_step_max_all_bodies": e["per_step_max_all_bodies"],
+                            "bodies_left_out_max": e["bodies_left_out_max"], "worst": e["worst"],
                             "free_running": e["free_running"], "check_s": round(time.perf_counter() - t0, 1),
                             "definition": "max |gpu - fp64| / max |fp64| over xyz; per step: each GPU step "
                                           "taken from the FP64 state rounded to FP32; free running: the GPU's "
@@ -796,6 +806,8 @@ def _extra_rigid_batched(args, dev, stream, out):
                         check_scenes=min(args.rb_check_scenes, args.rb_scenes), stream=stream)
         rbb["fp64_error"] = {"steps": e["steps"], "checked_scenes": min(args.rb_check_scenes, args.rb_scenes),
                              "checked_bodies": e["checked_bodies"], "per_step_max": e["per_step_max"],
+                             "per_step_max_all_bodies": e["per_step_max_all_bodies"],
+                             "bodies_left_out_max": e["bodies_left_out_max"], "worst": e["worst"],
                              "free_running": e["free_running"], "check_s": round(time.perf_counter() - t0, 1),
                              "definition": "as rigid.fp64_error, over the bodies of the first checked_scenes "
                                            "scenes of the batch (scenes never interact, so the oracle run on "
@@ -952,6 +964,8 @@ def main():
     ap.add_argument("--cell-factor", type=float, default=None,
                     help="sweep cell size / mean projected width (default: autotuned)")
     ap.add_argument("--sort-bits", type=int, default=None, choices=[24, 32], help="radix key width (default: autotuned)")
+    ap.add_argument("--sort", default=None, choices=["bucket", "radix"],
+                    help="how the sweep entries are sorted (default: autotuned)")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (defaults: 32 bits, cell factor 2.0)")
     ap.add_argument("--jitter-sets", type=int, default=N_JITTER,
                     help="distinct jittered inputs cycled by the timed calls (64 = the workload)")

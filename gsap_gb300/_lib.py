@@ -16,6 +16,7 @@ GSAP_OK = 0
 STATUS_NAMES = {0: "GSAP_OK", 1: "GSAP_ERR_INVALID", 2: "GSAP_ERR_CAPACITY", 3: "GSAP_ERR_CUDA",
                 4: "GSAP_ERR_DEVICE_TIMEOUT", 5: "GSAP_ERR_NONFINITE"}
 MODE_AABB, MODE_SPHERE = 0, 1
+SORT_RADIX, SORT_BUCKET = 0, 1
 AXIS_PCA, AXIS_REF = 0, 1
 FLAG_SORTED, FLAG_GRAPH, FLAG_TEMPORAL = 0x1, 0x2, 0x4
 CONTACT_REF, CONTACT_CONFIG = 0, 1
@@ -30,7 +31,7 @@ class GsapError(RuntimeError):
 class Config(C.Structure):
     _fields_ = [("mode", C.c_uint32), ("axis_mode", C.c_uint32), ("max_scenes", C.c_uint32),
                 ("entry_factor", C.c_uint32), ("pair_factor", C.c_uint32), ("sort_bits", C.c_uint32),
-                ("cell_factor", C.c_float), ("spin_limit", C.c_uint32)]
+                ("cell_factor", C.c_float), ("spin_limit", C.c_uint32), ("sort_mode", C.c_uint32)]
 
 
 class BodyData(C.Structure):

@@ -88,7 +88,7 @@ struct GraphShape {
     uint32_t n, S, flags, mode, both;
     uint32_t key_bits;
     float cell_factor;
-    uint32_t pad;
+    uint32_t sort_mode;
     uint64_t cap, ecap;
     bool operator==(const GraphShape& o) const { return memcmp(this, &o, sizeof(*this)) == 0; }
 };
@@ -131,7 +131,8 @@ static void free_scratch(gsap_sap* h) {
     BpScratch& s = h->s;
     void* ptrs[] = {s.ctrl, s.scenes, s.scenes_next, s.partials, s.scene_done, s.work_start, s.objscene,
                     s.keys[0], s.keys[1], s.vals[0], s.vals[1], s.status, s.rowcnt, s.rowoff, s.tmp_pairs,
-                    s.grp_pairs, s.tmp_rank, s.smin, s.smax, s.longrows, s.tile_sums};
+                    s.grp_pairs, s.tmp_rank, s.smin, s.smax, s.longrows, s.tile_sums, s.subcnt, s.substart,
+                    s.subsum};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (h->h_ctrl) cudaFreeHost(h->h_ctrl);
@@ -159,6 +160,10 @@ extern "C" gsap_sap* gsap_sap_create(uint32_t max_n, const gsap_config* cfg) {
     if (c.sort_bits != 24 && c.sort_bits != 32) { fail(GSAP_ERR_INVALID, "sort_bits must be 24 or 32"); return nullptr; }
     if (c.cell_factor <= 0.f) c.cell_factor = 2.0f;
     if (c.spin_limit == 0) c.spin_limit = kDefaultSpin;
+    if (c.sort_mode != GSAP_SORT_BUCKET && c.sort_mode != GSAP_SORT_RADIX) {
+        fail(GSAP_ERR_INVALID, "unknown sort_mode %u", c.sort_mode);
+        return nullptr;
+    }
     if (max_n == 0) max_n = 1;
     uint64_t ecap = (uint64_t)c.entry_factor * max_n + 4096;
     if (ecap >= (1ull << 30)) { fail(GSAP_ERR_INVALID, "entry capacity %llu exceeds 2^30", (unsigned long long)ecap); return nullptr; }
@@ -203,6 +208,10 @@ extern "C" gsap_sap* gsap_sap_create(uint32_t max_n, const gsap_config* cfg) {
     A((void**)&s.tmp_pairs, 8ull * s.pair_cap_internal);
     A((void**)&s.grp_pairs, 16ull * s.pair_cap_internal);  // both-direction form: two entries per pair
     A((void**)&s.tmp_rank, 8ull * s.pair_cap_internal);
+    A((void**)&s.subcnt, 4ull * kMaxSub);
+    A((void**)&s.substart, 4ull * (kMaxSub + 1));
+    A((void**)&s.subsum, 4ull * (kMaxSub / 4096));
+    if (ok && bucket_sort_setup() != cudaSuccess) ok = false;
     if (ok && cudaMallocHost((void**)&h->h_ctrl, 64) != cudaSuccess) ok = false;
     if (ok && cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking) != cudaSuccess) ok = false;
     for (auto& e : h->ev)
@@ -316,17 +325,23 @@ static gsap_status record(gsap_sap* h, const Call& c, cudaStream_t st, bool time
         CK(launch_pca(s, a, st));
     }
     mark();
-    CK(launch_project(s, a, passes, st));
+    const bool bucket = h->cfg.sort_mode == GSAP_SORT_BUCKET;
+    CK(launch_project(s, a, bucket ? 0 : passes, st));
     mark();
     const uint32_t* count = &s.ctrl->entry_count;
     int src = 0;
     SortGather gather{c.mn, c.mode == GSAP_MODE_AABB ? c.mx : nullptr, s.smin, s.smax};
-    for (int p = 0; p < passes; ++p) {
-        // the last pass's object ids go into the sweep records, not into a value array
-        const bool last = p == passes - 1;
-        CK(launch_sort_pass(s, p, passes, s.keys[src], s.vals[src], s.keys[src ^ 1], last ? nullptr : s.vals[src ^ 1],
-                            count, s.entry_cap, a.spin_limit, st, last ? &gather : nullptr, true));
-        src ^= 1;
+    if (bucket) {
+        CK(launch_bucket_sort(s, gather, a.spin_limit, st));  // sorted keys in keys[0]
+    } else {
+        for (int p = 0; p < passes; ++p) {
+            // the last pass's object ids go into the sweep records, not into a value array
+            const bool last = p == passes - 1;
+            CK(launch_sort_pass(s, p, passes, s.keys[src], s.vals[src], s.keys[src ^ 1],
+                                last ? nullptr : s.vals[src ^ 1], count, s.entry_cap, a.spin_limit, st,
+                                last ? &gather : nullptr, true));
+            src ^= 1;
+        }
     }
     mark();
     const bool canon = (c.flags & GSAP_FLAG_SORTED) || c.both;
@@ -361,6 +376,7 @@ static gsap_status run(gsap_sap* h, const Call& c, cudaStream_t st) {
     sh.n = c.n; sh.S = c.S; sh.flags = c.flags; sh.mode = (uint32_t)c.mode; sh.both = (uint32_t)c.both;
     sh.cap = c.cap; sh.ecap = c.ecap;
     sh.key_bits = h->cfg.sort_bits; sh.cell_factor = h->cfg.cell_factor;  // tuned settings are baked into a graph
+    sh.sort_mode = h->cfg.sort_mode;
     // LRU cache of captured pipelines, one per (inputs, outputs, sizes, flags)
     GraphEntry* hit = nullptr;
     size_t same = 0;
@@ -499,8 +515,9 @@ extern "C" gsap_status gsap_broadphase_aabb(gsap_sap* h, const float* d_min, con
     return broadphase(h, d_min, d_max, nullptr, 1, n, d_pairs, pair_cap, d_count, h_count, flags, stream);
 }
 
-// Times every (key width, cell factor) pair of a small grid on the caller's
-// input and keeps the fastest in the handle.  Key width sets the radix
+// Times every (sort, key width, cell factor) setting of a small grid on the
+// caller's input and keeps the fastest in the handle.  The sort is the
+// bucket sort or the onesweep radix passes; the key width sets the radix
 // passes (24 bits: three 8-bit digits, 32 bits: four) and the q resolution
 // of the sweep; the cell factor sets the cell edge on u2/u3 and with it the
 // replication (entries to sort) against the candidate run length (tests).
@@ -513,6 +530,7 @@ extern "C" gsap_status gsap_sap_autotune(gsap_sap* h, const float* d_min, const 
     if (reps < 1) reps = 1;
     if (d_scene_offsets && num_scenes == 0) return fail(GSAP_ERR_INVALID, "batched call needs scene offsets");
     const uint32_t S = d_scene_offsets ? num_scenes : 1;
+    const uint32_t sort_grid[2] = {GSAP_SORT_RADIX, GSAP_SORT_BUCKET};
     const uint32_t bits_grid[2] = {24, 32};
     const float cf_grid[5] = {1.0f, 1.5f, 2.0f, 2.5f, 3.0f};
     const gsap_config saved = h->cfg;
@@ -522,29 +540,32 @@ extern "C" gsap_status gsap_sap_autotune(gsap_sap* h, const float* d_min, const 
     CK(cudaEventCreate(&e1));
     float best_ms = -1.f;
     gsap_config best = saved;
-    for (uint32_t bits : bits_grid)
-        for (float cf : cf_grid) {
-            h->cfg.sort_bits = bits;
-            h->cfg.cell_factor = cf;
-            uint64_t cnt = 0;
-            // untimed first call: builds the graph and checks capacities
-            gsap_status r = broadphase(h, d_min, d_max, d_scene_offsets, S, n, d_pairs, pair_cap, nullptr, &cnt,
-                                       flags, stream);
-            if (r != GSAP_OK) continue;  // this setting does not fit the handle; try the next
-            cudaEventRecord(e0, st);
-            for (int k = 0; k < reps && r == GSAP_OK; ++k)
-                r = broadphase(h, d_min, d_max, d_scene_offsets, S, n, d_pairs, pair_cap, nullptr, nullptr, flags,
-                               stream);
-            cudaEventRecord(e1, st);
-            if (r == GSAP_OK) r = finish(h, st, &cnt, ~0ull);
-            float ms = 0.f;
-            if (r != GSAP_OK || cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
-                continue;
-            if (best_ms < 0.f || ms < best_ms) {
-                best_ms = ms;
-                best = h->cfg;
+    for (uint32_t sm : sort_grid)
+        for (uint32_t bits : bits_grid)
+            for (float cf : cf_grid) {
+                h->cfg.sort_mode = sm;
+                h->cfg.sort_bits = bits;
+                h->cfg.cell_factor = cf;
+                uint64_t cnt = 0;
+                // untimed first call: builds the graph and checks capacities
+                gsap_status r = broadphase(h, d_min, d_max, d_scene_offsets, S, n, d_pairs, pair_cap, nullptr, &cnt,
+                                           flags, stream);
+                if (r != GSAP_OK) continue;  // this setting does not fit the handle; try the next
+                cudaEventRecord(e0, st);
+                for (int k = 0; k < reps && r == GSAP_OK; ++k)
+                    r = broadphase(h, d_min, d_max, d_scene_offsets, S, n, d_pairs, pair_cap, nullptr, nullptr,
+                                   flags, stream);
+                cudaEventRecord(e1, st);
+                if (r == GSAP_OK) r = finish(h, st, &cnt, ~0ull);
+                float ms = 0.f;
+                if (r != GSAP_OK || cudaEventSynchronize(e1) != cudaSuccess ||
+                    cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+                    continue;
+                if (best_ms < 0.f || ms < best_ms) {
+                    best_ms = ms;
+                    best = h->cfg;
+                }
             }
-        }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     h->cfg = best;

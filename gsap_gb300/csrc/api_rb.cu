@@ -30,6 +30,7 @@ struct gsap_rb {
     int max_bodies, max_particles, max_pairs;
     int n_bodies, n_particles, n_shapes;
     float4 *pos, *quat, *lin, *ang;
+    float4* pos_lo;       // config model: low parts of the float-float body positions (zero after a set)
     int *shape, *pstart, *npart, *p_body;
     float* inv_mass;
     float4* inv_inertia;  // 3 rows per body
@@ -53,7 +54,7 @@ struct gsap_rb {
 };
 
 static void rb_free(gsap_rb* h) {
-    void* p[] = {h->pos, h->quat, h->lin, h->ang, h->shape, h->pstart, h->npart, h->p_body, h->inv_mass,
+    void* p[] = {h->pos, h->pos_lo, h->quat, h->lin, h->ang, h->shape, h->pstart, h->npart, h->p_body, h->inv_mass,
                  h->inv_inertia, h->p_pos, h->p_vel, h->p_force, h->p_rel, h->p_mass, h->ref_pos, h->ref_mass, h->shape_inv,
                  h->pairs, h->entries, h->bmin, h->bmax, h->body_pairs, h->scene_off, h->contacts};
     for (void* q : p)
@@ -77,7 +78,7 @@ extern "C" gsap_rb* gsap_rb_create(int32_t max_bodies, int32_t max_particles, in
         if (cudaMalloc(q, bytes) != cudaSuccess || cudaMemset(*q, 0, bytes) != cudaSuccess) ok = false;
     };
     size_t B = (size_t)max_bodies, Pn = (size_t)max_particles;
-    A((void**)&h->pos, 16 * B); A((void**)&h->quat, 16 * B); A((void**)&h->lin, 16 * B); A((void**)&h->ang, 16 * B);
+    A((void**)&h->pos, 16 * B); A((void**)&h->pos_lo, 16 * B); A((void**)&h->quat, 16 * B); A((void**)&h->lin, 16 * B); A((void**)&h->ang, 16 * B);
     A((void**)&h->shape, 4 * B); A((void**)&h->pstart, 4 * B); A((void**)&h->npart, 4 * B);
     A((void**)&h->p_body, 4 * Pn);
     A((void**)&h->inv_mass, 4 * B); A((void**)&h->inv_inertia, 48 * B);
@@ -145,6 +146,7 @@ extern "C" gsap_status gsap_rb_set_body_data(gsap_rb* h, const gsap_body_data* d
         if (pb[p] < 0) return set_error(GSAP_ERR_INVALID, "a particle belongs to no body");
     size_t B = (size_t)nb;
     RCK(cudaMemcpy(h->pos, d->pos, 16 * B, cudaMemcpyHostToDevice));
+    RCK(cudaMemset(h->pos_lo, 0, 16 * B));
     RCK(cudaMemcpy(h->quat, q.data(), 16 * B, cudaMemcpyHostToDevice));
     RCK(cudaMemcpy(h->lin, d->lin_vel, 16 * B, cudaMemcpyHostToDevice));
     RCK(cudaMemcpy(h->ang, d->ang_vel, 16 * B, cudaMemcpyHostToDevice));
@@ -179,6 +181,8 @@ extern "C" gsap_status gsap_rb_set_contact(gsap_rb* h, const gsap_contact_params
     if (!h || !p) return set_error(GSAP_ERR_INVALID, "null argument");
     if (p->model != GSAP_CONTACT_REF && p->model != GSAP_CONTACT_CONFIG)
         return set_error(GSAP_ERR_INVALID, "unknown contact model");
+    // the reference model steps plain FP32 positions: low parts start at zero
+    if (p->model != h->cp.model && h->max_bodies > 0) RCK(cudaMemset(h->pos_lo, 0, 16ull * h->max_bodies));
     h->cp = *p;
     return GSAP_OK;
 }
@@ -217,7 +221,8 @@ static CfgParams cfg_of(const gsap_rb* h, float dt) {
 extern "C" gsap_status gsap_rb_integrate(gsap_rb* h, float dt, void* stream) {
     if (!h) return set_error(GSAP_ERR_INVALID, "null handle");
     cudaStream_t st = (cudaStream_t)stream;
-    if (h->cp.model == GSAP_CONTACT_CONFIG) RCK(rb_integrate_cfg(h->pos, h->quat, h->lin, h->ang, cfg_of(h, dt), h->n_bodies, st));
+    if (h->cp.model == GSAP_CONTACT_CONFIG)
+        RCK(rb_integrate_cfg(h->pos, h->pos_lo, h->quat, h->lin, h->ang, cfg_of(h, dt), h->n_bodies, st));
     else RCK(rb_integrate_ref(h->pos, h->quat, h->lin, h->ang, dt, h->n_bodies, h->cp.gravity_y, (int)h->cp.floor_clamp, st));
     return GSAP_OK;
 }
@@ -276,7 +281,7 @@ extern "C" int32_t* gsap_rb_pair_entries(gsap_rb* h) { return h ? h->entries : n
 // and body-relative offsets before they are handed out.
 static void refresh_abs(gsap_rb* h, cudaStream_t st) {
     if (h->cp.model == GSAP_CONTACT_CONFIG && h->abs_stale) {
-        rb_abs_pos(h->pos, h->p_body, h->p_rel, h->p_pos, h->n_particles, st);
+        rb_abs_pos(h->pos, h->pos_lo, h->p_body, h->p_rel, h->p_pos, h->n_particles, st);
         cudaStreamSynchronize(st);
         h->abs_stale = false;
     }
@@ -323,16 +328,16 @@ extern "C" gsap_status gsap_rb_step(gsap_rb* h, gsap_sap* bp, float dt, void* st
     }
     // config model
     CfgParams p = cfg_of(h, dt);
-    RCK(rb_integrate_cfg(h->pos, h->quat, h->lin, h->ang, p, h->n_bodies, st));
+    RCK(rb_integrate_cfg(h->pos, h->pos_lo, h->quat, h->lin, h->ang, p, h->n_bodies, st));
     RCK(rb_place_cfg(h->quat, h->lin, h->ang, h->shape, h->pstart, h->p_body, h->ref_pos, h->p_rel, h->p_vel,
                      h->n_particles, st));
     h->abs_stale = true;
-    RCK(rb_body_aabb(h->pos, h->p_rel, h->pstart, h->npart, h->bmin, h->bmax, h->n_bodies, st));
+    RCK(rb_body_aabb(h->pos, h->pos_lo, h->p_rel, h->pstart, h->npart, h->bmin, h->bmax, h->n_bodies, st));
     BpDeviceCounts dc;
     r = bp_both_async(bp, GSAP_MODE_AABB, h->bmin, h->bmax, h->scene_off, h->num_scenes ? h->num_scenes : 1,
                       (uint32_t)h->n_bodies, h->body_pairs, h->body_pair_cap, nullptr, 0, st, &dc, GSAP_FLAG_TEMPORAL);
     if (r != GSAP_OK) return r;
-    RCK(rb_forces_cfg(h->pos, h->p_rel, h->p_vel, h->p_body, h->pstart, h->npart, h->body_pairs, dc.rowoff,
+    RCK(rb_forces_cfg(h->pos, h->pos_lo, h->p_rel, h->p_vel, h->p_body, h->pstart, h->npart, h->body_pairs, dc.rowoff,
                       h->body_pair_cap, p, h->p_force, h->n_particles, st));
     RCK(rb_update_cfg(h->lin, h->ang, h->quat, h->inv_mass, h->shape, h->pstart, h->npart, h->ref_pos, h->shape_inv,
                       h->p_force, p, h->n_bodies, st));
@@ -356,7 +361,10 @@ extern "C" gsap_status gsap_rb_set_state(gsap_rb* h, const float* pos, const flo
     if (!h) return set_error(GSAP_ERR_INVALID, "null handle");
     cudaStream_t st = (cudaStream_t)stream;
     size_t B = 16ull * h->n_bodies;
-    if (pos) RCK(cudaMemcpyAsync(h->pos, pos, B, cudaMemcpyHostToDevice, st));
+    if (pos) {
+        RCK(cudaMemcpyAsync(h->pos, pos, B, cudaMemcpyHostToDevice, st));
+        RCK(cudaMemsetAsync(h->pos_lo, 0, B, st));
+    }
     if (quat) RCK(cudaMemcpyAsync(h->quat, quat, B, cudaMemcpyHostToDevice, st));
     if (lin) RCK(cudaMemcpyAsync(h->lin, lin, B, cudaMemcpyHostToDevice, st));
     if (ang) RCK(cudaMemcpyAsync(h->ang, ang, B, cudaMemcpyHostToDevice, st));
@@ -429,7 +437,7 @@ extern "C" gsap_status gsap_k_integrate(float* pos, float* quat, float* lin, flo
         memset(&c, 0, sizeof(c));
         c.dt = dt;
         c.gy = p->gravity_y;
-        RCK(rb_integrate_cfg((float4*)pos, (float4*)quat, (float4*)lin, (const float4*)ang, c, n, st));
+        RCK(rb_integrate_cfg((float4*)pos, nullptr, (float4*)quat, (float4*)lin, (const float4*)ang, c, n, st));
     } else {
         RCK(rb_integrate_ref((float4*)pos, (float4*)quat, (float4*)lin, (float4*)ang, dt, n, p->gravity_y,
                              (int)p->floor_clamp, st));

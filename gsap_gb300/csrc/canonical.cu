@@ -197,15 +197,53 @@ __global__ void __launch_bounds__(kThreads) k_rowsum(const uint32_t* __restrict_
     if (threadIdx.x == 0) tsum[blockIdx.x] = t;
 }
 
+// Many tiles (n above kDirectTiles * 4096 rows): the tile sums are scanned
+// once, in place, by one CTA (k_tilescan) instead of every tile summing all
+// the sums before its own, which grows with the square of the tile count.
+constexpr uint32_t kDirectTiles = 512;
+
+__global__ void __launch_bounds__(1024) k_tilescan(uint32_t* tsum, uint32_t ntiles) {
+    __shared__ uint32_t s_w[32];
+    __shared__ uint32_t s_carry;
+    const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (tid == 0) s_carry = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < ntiles; base += 1024) {
+        const uint32_t i = base + tid;
+        const uint32_t v = i < ntiles ? tsum[i] : 0u;
+        uint32_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        if (lane == 31) s_w[wid] = x;
+        __syncthreads();
+        uint32_t pre = 0;
+        for (uint32_t w = 0; w < wid; ++w) pre += s_w[w];
+        const uint32_t excl = s_carry + pre + x - v;
+        if (i < ntiles) tsum[i] = excl;
+        __syncthreads();
+        if (tid == 1023) s_carry = excl + v;
+        __syncthreads();
+    }
+}
+
+// scanned != 0: tsum holds every tile's exclusive offset (k_tilescan ran).
 __global__ void __launch_bounds__(kThreads) k_rowscan(uint32_t* in, uint32_t* out, const uint32_t* __restrict__ tsum,
-                                                      uint32_t n) {
+                                                      uint32_t n, int scanned) {
     __shared__ uint32_t s_w[kThreads / 32];
     const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const uint32_t t = blockIdx.x;
     // offset of this tile: the sums of all tiles before it
-    uint32_t ps = 0;
-    for (uint32_t k = tid; k < t; k += kThreads) ps += tsum[k];
-    const uint32_t tile_off = cta_sum256(ps, s_w);
+    uint32_t tile_off;
+    if (scanned) {
+        tile_off = tsum[t];
+    } else {
+        uint32_t ps = 0;
+        for (uint32_t k = tid; k < t; k += kThreads) ps += tsum[k];
+        tile_off = cta_sum256(ps, s_w);
+    }
     const uint32_t b = t * kScanTile + tid * kScanItems;
     uint32_t v[kScanItems];
     const bool full = b + kScanItems <= n;
@@ -396,7 +434,9 @@ cudaError_t launch_canonical(const BpScratch& s, uint32_t n, const uint2* in_pai
     const int grid = sm_count() * 4;
     const uint32_t ntiles = (n + kScanTile - 1) / kScanTile;
     k_rowsum<<<ntiles, kThreads, 0, st>>>(s.rowcnt, s.tile_sums, n);
-    k_rowscan<<<ntiles, kThreads, 0, st>>>(s.rowcnt, s.rowoff, s.tile_sums, n);
+    const int scanned = ntiles > kDirectTiles ? 1 : 0;
+    if (scanned) k_tilescan<<<1, 1024, 0, st>>>(s.tile_sums, ntiles);
+    k_rowscan<<<ntiles, kThreads, 0, st>>>(s.rowcnt, s.rowoff, s.tile_sums, n, scanned);
     const uint64_t grp_cap = 2 * s.pair_cap_internal;
     k_scatter<<<sm_count() * 16, kThreads, 0, st>>>(s, in_pairs, in_cap, s.grp_pairs, grp_cap, both);
     k_rank<<<sm_count() * 8, kThreads, 0, st>>>(s, s.grp_pairs, grp_cap, n, out_pairs, out_cap);

@@ -26,6 +26,12 @@ constexpr int kMaxPasses = 4;         // radix passes (8-bit digits, <= 32-bit k
 constexpr int kSortItems = 16;        // keys per thread in a onesweep tile
 constexpr int kSortTile = kThreads * kSortItems;
 constexpr uint32_t kDefaultSpin = 1u << 24;
+// Bucket sort: a sub-bucket is a cell together with the top T bits of the
+// quantised lower bound, i.e. the top bits of the key above `shift`; at most
+// kMaxSub of them (the key layout keeps the cells at or below 2^20).
+constexpr uint32_t kMaxSubBits = 20;
+constexpr uint32_t kMaxSub = 1u << kMaxSubBits;
+constexpr uint32_t kSubTopBits = 4;
 
 // Sticky device error bits (ctrl->error).
 enum : uint32_t {
@@ -131,6 +137,11 @@ struct BpScratch {
     uint2* grp_pairs;          // pairs grouped by row, before the in-row order (canonical output)
     uint32_t* tmp_rank;        // per unsorted pair k: its slot in row first (rank[k]); both-direction
                                // form: slots in row first and row second (rank[2k], rank[2k + 1])
+    // bucket sort: entries per sub-bucket (zero between calls), their
+    // exclusive offsets (M + 1), per-4096 sums of the offset scan
+    uint32_t* subcnt;
+    uint32_t* substart;
+    uint32_t* subsum;
     uint64_t entry_cap;
     uint64_t pair_cap_internal;
     uint64_t status_words;
@@ -184,6 +195,36 @@ cudaError_t launch_sort_pass(const BpScratch& s, int pass, int passes, const uin
 // of the float images of the keys).
 cudaError_t launch_sort_prep(const BpScratch& s, const uint32_t* keys, const uint32_t* count_ptr,
                              uint32_t n, int passes, cudaStream_t st, int flip = 0);
+// Bucket sort of the projection's entries (keys[0] / vals[0], counted per
+// sub-bucket by the projection): scan of the sub-bucket counts, scatter into
+// sub-buckets (keys[1] / vals[1]), local sort of every sub-bucket; the
+// sorted keys end in keys[0] and the entry records in G.smin / G.smax.
+cudaError_t launch_bucket_sort(const BpScratch& s, const SortGather& G, uint32_t spin, cudaStream_t st);
+// Per-device set-up of the bucket sort's launch (kernel attributes); called
+// when a handle is created, outside any stream capture.
+cudaError_t bucket_sort_setup();
+
+// Sub-bucket layout of a key layout: sub-bucket id = key >> shift, `count`
+// sub-buckets (a cell and the top T <= kSubTopBits bits of its quantised
+// lower bound, T chosen so that count <= kMaxSub).
+struct SubLayout {
+    uint32_t shift, count;
+};
+__host__ __device__ inline SubLayout sub_layout_of(uint32_t Q, uint32_t total_buckets) {
+    uint32_t bb = 0;
+    while (bb < 32 && (1ull << bb) < (uint64_t)total_buckets) ++bb;
+    int T = (int)kSubTopBits;
+    if (T > (int)Q) T = (int)Q;
+    if (T > (int)kMaxSubBits - (int)bb) T = (int)kMaxSubBits - (int)bb;
+    if (T < 0) T = 0;
+    SubLayout L;
+    L.shift = Q - (uint32_t)T;
+    L.count = total_buckets << T;
+    return L;
+}
+#ifdef __CUDACC__
+__device__ inline SubLayout sub_layout(const Ctrl* C) { return sub_layout_of(C->qbits, C->total_buckets); }
+#endif
 cudaError_t launch_sweep(const BpScratch& s, const BpArgs& a, const uint32_t* keys,
                          uint2* pairs, uint64_t pair_cap, int count_rows, cudaStream_t st);
 cudaError_t launch_canonical(const BpScratch& s, uint32_t n, const uint2* in_pairs, uint64_t in_cap,
@@ -253,6 +294,46 @@ __device__ __forceinline__ uint32_t lookback(uint64_t* status, uint32_t tile, ui
         }
     }
     return excl;
+}
+
+// u . x over the box spanned by corners a, b (any order), rounded outward:
+// [lo, hi] contains the exact projection of the box.
+__device__ __forceinline__ void project_box(const float* u, float3 a, float3 b, float& lo, float& hi) {
+    float l0 = fminf(__fmul_rd(u[0], a.x), __fmul_rd(u[0], b.x));
+    float l1 = fminf(__fmul_rd(u[1], a.y), __fmul_rd(u[1], b.y));
+    float l2 = fminf(__fmul_rd(u[2], a.z), __fmul_rd(u[2], b.z));
+    float h0 = fmaxf(__fmul_ru(u[0], a.x), __fmul_ru(u[0], b.x));
+    float h1 = fmaxf(__fmul_ru(u[1], a.y), __fmul_ru(u[1], b.y));
+    float h2 = fmaxf(__fmul_ru(u[2], a.z), __fmul_ru(u[2], b.z));
+    lo = __fadd_rd(__fadd_rd(l0, l1), l2);
+    hi = __fadd_ru(__fadd_ru(h0, h1), h2);
+}
+
+// Box of a sphere (centre, radius in w): centre -/+ |r|, rounded outward.
+__device__ __forceinline__ void sphere_box(float4 p, float3& a, float3& b) {
+    const float r = fabsf(p.w);
+    a = make_float3(__fsub_rd(p.x, r), __fsub_rd(p.y, r), __fsub_rd(p.z, r));
+    b = make_float3(__fadd_ru(p.x, r), __fadd_ru(p.y, r), __fadd_ru(p.z, r));
+}
+
+// Sweep records of sorted entry g (value = object index | owner flags <<
+// kFlagShift), written by the last step of either sort: the bounds of its
+// object (boxes: (lo.xyz, object index), (hi.xyz, owner flags); spheres:
+// (centre, radius), (object index, owner flags, 0, 0)).
+__device__ __forceinline__ void put_record(const BpScratch& S, const SortGather& G, uint32_t g, uint32_t key,
+                                           uint32_t val) {
+    (void)S;
+    (void)key;
+    const uint32_t obj = val & kObjMask, fl = val >> kFlagShift;
+    const float4 lo = __ldg(G.mn + obj);
+    if (G.mx) {  // boxes: index and flags ride in the unused w lanes
+        const float4 hi = __ldg(G.mx + obj);
+        G.smin[g] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(obj));
+        G.smax[g] = make_float4(hi.x, hi.y, hi.z, __uint_as_float(fl));
+    } else {     // spheres: radius in w, index and flags in the second record
+        G.smin[g] = lo;
+        G.smax[g] = make_float4(__uint_as_float(obj), __uint_as_float(fl), 0.f, 0.f);
+    }
 }
 
 // Error-free transformation a + b = s + e (Knuth two-sum).

@@ -361,6 +361,121 @@ __global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, 
     for (uint32_t s = tid; s < A.num_scenes; s += kThreads) out[s].q_scale = __fdiv_rn(qf, __ldcg(&out[s].q_range));
 }
 
+// Batched form of the finish (more than one scene).  A CTA takes
+// kFinishScenes consecutive scenes: each of its warps merges the partials of
+// some of them (lane l merges items l, l+32, ... in float-float, then a fixed
+// shuffle tree, so the result does not depend on timing), and warp 0 then
+// solves all of them side by side, one scene per lane.  GB300 issues an FP64
+// warp instruction at a small fraction of the FP32 rate however few of its
+// lanes are active, so solving 32 scenes per warp instruction rather than
+// one cuts the FP64 time of a batch about 32-fold.  The last CTA to finish
+// lays out the keys and resets the counters, as k_pca_finish does.
+constexpr int kFinishWarps = 16;
+constexpr int kFinishScenes = 32;
+__global__ void __launch_bounds__(32 * kFinishWarps) k_pca_finish_batch(BpScratch S, BpArgs A, uint64_t entry_cap,
+                                                                       int temporal) {
+    __shared__ SceneSums s_z[kFinishScenes];
+    Scene* const out = temporal ? S.scenes_next : S.scenes;
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t s0 = blockIdx.x * kFinishScenes;
+    Ctrl* C = S.ctrl;
+    for (uint32_t k = wid; k < (uint32_t)kFinishScenes; k += kFinishWarps) {
+        const uint32_t scene = s0 + k;
+        if (scene >= A.num_scenes) break;
+        const uint32_t sb = scene_begin(A, scene), se = scene_end(A, scene);
+        const uint32_t wfirst = S.work_start[scene];
+        const uint32_t nw0 = S.work_start[scene + 1] - wfirst;
+        const uint32_t nw = wfirst < A.num_work ? min(nw0, A.num_work - wfirst) : 0u;
+        float px = 0.f, py = 0.f, pz = 0.f;
+        if (lane == 0) pilot_of(A, sb, se, px, py, pz);
+        float ah[kPcaQ], al[kPcaQ], am[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int q = 0; q < kPcaQ; ++q) { ah[q] = 0.f; al[q] = 0.f; }
+        for (uint32_t j = lane; j < nw; j += 32) {
+            const PcaPartial* P = &S.partials[wfirst + j];
+#pragma unroll
+            for (int q = 0; q < kPcaQ; ++q) kahan_merge(ah[q], al[q], P->hi[q], P->lo[q]);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) am[q] = fmaxf(am[q], P->hmax[q]);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int q = 0; q < kPcaQ; ++q) {
+                float h2 = __shfl_down_sync(0xffffffffu, ah[q], o);
+                float l2 = __shfl_down_sync(0xffffffffu, al[q], o);
+                kahan_merge(ah[q], al[q], h2, l2);
+            }
+#pragma unroll
+            for (int q = 0; q < 3; ++q) am[q] = fmaxf(am[q], __shfl_down_sync(0xffffffffu, am[q], o));
+        }
+        if (lane == 0) {
+            SceneSums& z = s_z[k];
+            for (int q = 0; q < 3; ++q) {
+                z.sd[q] = (double)ah[q] + (double)al[q];
+                z.sh[q] = (double)ah[9 + q] + (double)al[9 + q];
+                z.hmax[q] = (double)am[q];
+            }
+            for (int q = 0; q < 6; ++q) {
+                z.sdd[q] = (double)ah[3 + q] + (double)al[3 + q];
+                z.shh[q] = (double)ah[12 + q] + (double)al[12 + q];
+            }
+            z.pilot[0] = px; z.pilot[1] = py; z.pilot[2] = pz;
+            z.n = (double)(se - sb);
+        }
+    }
+    __syncthreads();
+    if (wid != 0) return;
+    const uint32_t cnt = min((uint32_t)kFinishScenes, A.num_scenes - s0);
+    if (lane < cnt) {
+        Scene sc;
+        choose_scene(s_z[lane], A, entry_cap, A.n, sc);
+        out[s0 + lane] = sc;
+    }
+    __threadfence();
+    __syncwarp();
+    uint32_t last = 0;
+    if (lane == 0) last = atomicAdd(&C->scenes_done, cnt) + cnt == A.num_scenes ? 1u : 0u;
+    last = __shfl_sync(0xffffffffu, last, 0);
+    if (!last) return;
+    __threadfence();  // the other scenes' records are read below
+    // Last scene: global bucket bases, key layout, counter reset.
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < A.num_scenes; base += 32) {
+        const uint32_t s = base + lane;
+        const uint32_t v = s < A.num_scenes ? __ldcg(&out[s].G2) * __ldcg(&out[s].G3) : 0u;
+        uint32_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        if (s < A.num_scenes) out[s].bucket_base = carry + x - v;
+        carry += __shfl_sync(0xffffffffu, x, 31);
+    }
+    const uint32_t total = carry;
+    const uint32_t q = key_q_bits(A.key_bits, total);
+    if (lane == 0) {
+        if (q == 0) atomicOr(&C->error, kErrCellRange);
+        C->scenes_done = 0;
+        if (temporal) {
+            C->qbits_next = q;
+            C->key_bits_next = A.key_bits;
+            C->total_buckets_next = total;
+        } else {
+            C->qbits = q;
+            C->key_bits = A.key_bits;
+            C->total_buckets = total;
+            reset_counters(C);
+            C->epoch = C->epoch + 1u;
+        }
+    }
+    if (!temporal)
+        for (uint32_t k = lane; k < (uint32_t)kMaxPasses * 256u; k += 32) (&C->hist[0][0])[k] = 0u;
+    const float qf = (float)(1u << q);
+    for (uint32_t s = lane; s < A.num_scenes; s += 32) out[s].q_scale = __fdiv_rn(qf, __ldcg(&out[s].q_range));
+}
+
 cudaError_t launch_plan(const BpScratch& s, const BpArgs& a, cudaStream_t st) {
     k_plan<<<1, 1024, 0, st>>>(s, a);
     return cudaGetLastError();
@@ -368,7 +483,11 @@ cudaError_t launch_plan(const BpScratch& s, const BpArgs& a, cudaStream_t st) {
 
 cudaError_t launch_pca(const BpScratch& s, const BpArgs& a, cudaStream_t st, int temporal) {
     k_pca<<<a.num_work, kThreads, 0, st>>>(s, a);
-    k_pca_finish<<<a.num_scenes, kThreads, 0, st>>>(s, a, s.entry_cap, temporal);
+    if (a.num_scenes > 1)
+        k_pca_finish_batch<<<(a.num_scenes + kFinishScenes - 1) / kFinishScenes, 32 * kFinishWarps, 0, st>>>(
+            s, a, s.entry_cap, temporal);
+    else
+        k_pca_finish<<<1, kThreads, 0, st>>>(s, a, s.entry_cap, temporal);
     return cudaGetLastError();
 }
 
@@ -387,8 +506,12 @@ __global__ void k_reset(BpScratch S) {
 // Temporal mode, after both branches: the parameters computed from this
 // call's input become the ones the next call uses.
 __global__ void k_commit(BpScratch S, uint32_t num_scenes) {
-    for (uint32_t s = threadIdx.x; s < num_scenes; s += blockDim.x) S.scenes[s] = S.scenes_next[s];
-    if (threadIdx.x == 0) {
+    // the records as 8-byte words, one per thread (coalesced)
+    static_assert(sizeof(Scene) % 8 == 0, "Scene is copied in 8-byte words");
+    const uint64_t words = (uint64_t)num_scenes * (sizeof(Scene) / 8);
+    const uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (w < words) reinterpret_cast<uint64_t*>(S.scenes)[w] = reinterpret_cast<const uint64_t*>(S.scenes_next)[w];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
         Ctrl* C = S.ctrl;
         C->qbits = C->qbits_next;
         C->key_bits = C->key_bits_next;
@@ -402,7 +525,8 @@ cudaError_t launch_reset(const BpScratch& s, cudaStream_t st) {
 }
 
 cudaError_t launch_commit(const BpScratch& s, uint32_t num_scenes, cudaStream_t st) {
-    k_commit<<<1, 256, 0, st>>>(s, num_scenes);
+    const uint64_t words = (uint64_t)num_scenes * (sizeof(Scene) / 8);
+    k_commit<<<(unsigned)((words + 255) / 256), 256, 0, st>>>(s, num_scenes);
     return cudaGetLastError();
 }
 

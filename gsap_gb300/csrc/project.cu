@@ -18,18 +18,6 @@
 
 namespace gsap {
 
-// u.x over the box spanned by corners a, b (any order), rounded outward.
-__device__ __forceinline__ void project_box(const float* u, float3 a, float3 b, float& lo, float& hi) {
-    float l0 = fminf(__fmul_rd(u[0], a.x), __fmul_rd(u[0], b.x));
-    float l1 = fminf(__fmul_rd(u[1], a.y), __fmul_rd(u[1], b.y));
-    float l2 = fminf(__fmul_rd(u[2], a.z), __fmul_rd(u[2], b.z));
-    float h0 = fmaxf(__fmul_ru(u[0], a.x), __fmul_ru(u[0], b.x));
-    float h1 = fmaxf(__fmul_ru(u[1], a.y), __fmul_ru(u[1], b.y));
-    float h2 = fmaxf(__fmul_ru(u[2], a.z), __fmul_ru(u[2], b.z));
-    lo = __fadd_rd(__fadd_rd(l0, l1), l2);
-    hi = __fadd_ru(__fadd_ru(h0, h1), h2);
-}
-
 // Clamped monotone cell index.
 __device__ __forceinline__ uint32_t cell_of(float x, float org, float inv, uint32_t G) {
     float t = __fmul_rn(__fsub_rn(x, org), inv);
@@ -45,9 +33,7 @@ __device__ __forceinline__ bool load_box(const BpArgs& A, uint32_t i, float3& a,
         a = make_float3(p.x, p.y, p.z);
         b = make_float3(q.x, q.y, q.z);
     } else {
-        float r = fabsf(p.w);
-        a = make_float3(__fsub_rd(p.x, r), __fsub_rd(p.y, r), __fsub_rd(p.z, r));
-        b = make_float3(__fadd_ru(p.x, r), __fadd_ru(p.y, r), __fadd_ru(p.z, r));
+        sphere_box(p, a, b);
     }
     return isfinite(a.x) && isfinite(a.y) && isfinite(a.z) && isfinite(b.x) && isfinite(b.y) && isfinite(b.z);
 }
@@ -56,9 +42,12 @@ constexpr int kProjItems = 8;                          // objects per thread
 constexpr int kProjHalf = kThreads * kProjItems;       // objects per CTA: half a work chunk
 constexpr int kProjSplit = kChunk / kProjHalf;         // CTAs per work chunk
 
+// PASSES > 0: counts the first radix digit for the onesweep passes;
+// PASSES == 0 (bucket sort): counts the entries of every sub-bucket instead
+// (global atomics; sub_layout in internal.cuh).
 template <int PASSES>
 __global__ void __launch_bounds__(kThreads) k_project(BpScratch S, BpArgs A) {
-    __shared__ uint32_t s_hist[PASSES][256];
+    __shared__ uint32_t s_hist[PASSES > 0 ? PASSES : 1][256];
     __shared__ float s_f[16];
     __shared__ uint32_t s_i[4];
     __shared__ uint32_t s_wtot[kThreads / 32];
@@ -66,7 +55,7 @@ __global__ void __launch_bounds__(kThreads) k_project(BpScratch S, BpArgs A) {
     const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     uint32_t scene, b, e, wfirst, nw;
     if (!map_work(blockIdx.x / kProjSplit, S, A, scene, b, e, wfirst, nw)) return;
-    for (uint32_t k = tid; k < PASSES * 256; k += kThreads) (&s_hist[0][0])[k] = 0u;
+    for (uint32_t k = tid; k < 256u * (PASSES > 0 ? PASSES : 1); k += kThreads) (&s_hist[0][0])[k] = 0u;
     if (tid == 0) {
         const Scene& sc = S.scenes[scene];
         for (int k = 0; k < 9; ++k) s_f[k] = sc.u[k];
@@ -84,6 +73,7 @@ __global__ void __launch_bounds__(kThreads) k_project(BpScratch S, BpArgs A) {
     }
     __syncthreads();
     const uint32_t G2 = s_i[0], G3 = s_i[1], bb = s_i[2], Q = s_i[3];
+    const uint32_t sub_shift = PASSES == 0 ? sub_layout(S.ctrl).shift : 0u;
     const float qmax = (float)((1u << Q) - 1u);
 
     bool bad = false;
@@ -152,21 +142,24 @@ __global__ void __launch_bounds__(kThreads) k_project(BpScratch S, BpArgs A) {
                     const uint32_t fl = (x2 == 0 ? 1u : 0u) | (x3 == 0 ? 2u : 0u);
                     S.keys[0][pos] = key;
                     S.vals[0][pos] = i | (fl << kFlagShift);
-                    atomicAdd(&s_hist[0][key & 255u], 1u);  // later digits: counted by the sort passes
+                    if (PASSES > 0) atomicAdd(&s_hist[0][key & 255u], 1u);  // later digits: counted by the sort passes
+                    else atomicAdd(&S.subcnt[min(key >> sub_shift, kMaxSub - 1u)], 1u);
                 }
             }
     }
     }
     if (bad) atomicOr(&S.ctrl->error, kErrNonFinite);
     __syncthreads();
-    for (uint32_t k = tid; k < 256; k += kThreads) {
-        uint32_t v = s_hist[0][k];
-        if (v) atomicAdd(&S.ctrl->hist[0][k], v);
-    }
+    if (PASSES > 0)
+        for (uint32_t k = tid; k < 256; k += kThreads) {
+            uint32_t v = s_hist[0][k];
+            if (v) atomicAdd(&S.ctrl->hist[0][k], v);
+        }
 }
 
 cudaError_t launch_project(const BpScratch& s, const BpArgs& a, int passes, cudaStream_t st) {
-    if (passes == 3) k_project<3><<<a.num_work * kProjSplit, kThreads, 0, st>>>(s, a);
+    if (passes == 0) k_project<0><<<a.num_work * kProjSplit, kThreads, 0, st>>>(s, a);
+    else if (passes == 3) k_project<3><<<a.num_work * kProjSplit, kThreads, 0, st>>>(s, a);
     else k_project<4><<<a.num_work * kProjSplit, kThreads, 0, st>>>(s, a);
     return cudaGetLastError();
 }

@@ -34,18 +34,21 @@ struct CfgParams {
     float lo[3], hi[3];
     unsigned long long* contacts;  // if set: += particle-particle contacts, counted from both sides
 };
-cudaError_t rb_integrate_cfg(float4* pos, float4* quat, float4* lin, const float4* ang, const CfgParams& p, int n,
-                             cudaStream_t st);
+// pos_lo: the low parts of the float-float body positions (nullptr: plain
+// FP32 positions)
+cudaError_t rb_integrate_cfg(float4* pos, float4* pos_lo, float4* quat, float4* lin, const float4* ang,
+                             const CfgParams& p, int n, cudaStream_t st);
 cudaError_t rb_place_cfg(const float4* quat, const float4* lin, const float4* ang, const int* shape,
                          const int* pstart, const int* p_body, const float4* ref_pos, float4* p_rel, float4* p_vel,
                          int np, cudaStream_t st);
-cudaError_t rb_abs_pos(const float4* pos, const int* p_body, const float4* p_rel, float4* p_pos, int np,
-                       cudaStream_t st);
-cudaError_t rb_body_aabb(const float4* pos, const float4* p_rel, const int* pstart, const int* npart, float4* bmin,
-                         float4* bmax, int n, cudaStream_t st);
-cudaError_t rb_forces_cfg(const float4* pos, const float4* p_rel, const float4* p_vel, const int* p_body,
-                          const int* pstart, const int* npart, const uint2* body_pairs, const uint32_t* rowoff,
-                          uint64_t pair_cap, const CfgParams& p, float4* p_force, int np, cudaStream_t st);
+cudaError_t rb_abs_pos(const float4* pos, const float4* pos_lo, const int* p_body, const float4* p_rel, float4* p_pos,
+                       int np, cudaStream_t st);
+cudaError_t rb_body_aabb(const float4* pos, const float4* pos_lo, const float4* p_rel, const int* pstart,
+                         const int* npart, float4* bmin, float4* bmax, int n, cudaStream_t st);
+cudaError_t rb_forces_cfg(const float4* pos, const float4* pos_lo, const float4* p_rel, const float4* p_vel,
+                          const int* p_body, const int* pstart, const int* npart, const uint2* body_pairs,
+                          const uint32_t* rowoff, uint64_t pair_cap, const CfgParams& p, float4* p_force, int np,
+                          cudaStream_t st);
 cudaError_t rb_update_cfg(float4* lin, float4* ang, const float4* quat, const float* inv_mass, const int* shape,
                           const int* pstart, const int* npart, const float4* ref_pos, const float4* shape_inv,
                           const float4* p_force, const CfgParams& p, int n, cudaStream_t st);

@@ -18,13 +18,18 @@
 // thread per body for the body AABB and for the compensated (two-sum)
 // per-body force / torque reduction fused with the velocity update.
 //
-// Precision: particles are kept as body-relative offsets r = R ref (|r| <= a
-// few units) next to the FP32 body positions x.  A particle-particle vector
-// is formed as (x_b - x_a) + (r_j - r_i): the body difference is exact or
-// nearly so for touching bodies, so the penetration depth keeps ~1e-7
-// absolute accuracy instead of the ~4e-6 an absolute FP32 coordinate near
-// 100 would give it.  Absolute particle positions are produced only when the
-// caller reads them.
+// Precision: a body position is a float-float pair x = hi + lo (hi is the
+// FP32 position the caller sees, lo the rounding error that the FP32 update
+// x += v dt leaves, carried from step to step; lo = 0 after the caller sets
+// a position), and particles are kept as body-relative offsets r = R ref
+// (|r| <= a few units).  A particle-particle vector is formed as
+// (hi_b - hi_a) + (lo_b - lo_a) + (r_j - r_i): the difference of the high
+// parts is exact for touching bodies (Sterbenz), so the penetration depth
+// keeps ~1e-7 absolute accuracy.  With plain FP32 positions near 100 the
+// rounding of every position update alone moves a contact by up to half an
+// ulp (~4e-6), which the stiff spring turns into a force error of k * 4e-6
+// -- several times the 1e-5 relative velocity error allowed per step.
+// Absolute particle positions are produced only when the caller reads them.
 #include "internal.cuh"
 #include "rigid.cuh"
 
@@ -44,7 +49,20 @@ __device__ __forceinline__ float3 cross3(float3 a, float3 b) {
     return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
 
-__global__ void k_integrate_cfg(float4* pos, float4* quat, float4* lin, const float4* ang, CfgParams p, int n) {
+// (hi, lo) += d, renormalised so that hi = fl(hi + lo): two-sum of hi and d,
+// the error joined to lo, then a fast two-sum (|s| >= |l| up to rounding
+// for any |lo| < ulp(hi)).
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float d) {
+    const float s = __fadd_rn(hi, d);
+    const float bb = __fsub_rn(s, hi);
+    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(d, bb));
+    const float l = __fadd_rn(lo, e);
+    hi = __fadd_rn(s, l);
+    lo = __fsub_rn(l, __fsub_rn(hi, s));
+}
+
+__global__ void k_integrate_cfg(float4* pos, float4* pos_lo, float4* quat, float4* lin, const float4* ang,
+                                CfgParams p, int n) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= n) return;
     float4 v = lin[b];
@@ -62,7 +80,15 @@ __global__ void k_integrate_cfg(float4* pos, float4* quat, float4* lin, const fl
     q.x *= il; q.y *= il; q.z *= il; q.w *= il;
     quat[b] = q;
     float4 x = pos[b];
-    x.x += v.x * p.dt; x.y += v.y * p.dt; x.z += v.z * p.dt;
+    if (pos_lo) {
+        float4 l = pos_lo[b];
+        ff_add(x.x, l.x, v.x * p.dt);
+        ff_add(x.y, l.y, v.y * p.dt);
+        ff_add(x.z, l.z, v.z * p.dt);
+        pos_lo[b] = l;
+    } else {
+        x.x += v.x * p.dt; x.y += v.y * p.dt; x.z += v.z * p.dt;
+    }
     pos[b] = x;
 }
 
@@ -82,31 +108,33 @@ __global__ void k_place_cfg(const float4* quat, const float4* lin, const float4*
     p_vel[i] = make_float4(v.x + wr.x, v.y + wr.y, v.z + wr.z, 0.f);
 }
 
-// absolute particle positions (readback only)
-__global__ void k_abs_pos(const float4* pos, const int* p_body, const float4* p_rel, float4* p_pos, int np) {
+// absolute particle positions (readback only): hi + (lo + r)
+__global__ void k_abs_pos(const float4* pos, const float4* pos_lo, const int* p_body, const float4* p_rel,
+                          float4* p_pos, int np) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= np) return;
-    float4 x = pos[p_body[i]], r = p_rel[i];
-    p_pos[i] = make_float4(x.x + r.x, x.y + r.y, x.z + r.z, r.w);
+    const int b = p_body[i];
+    float4 x = pos[b], l = pos_lo[b], r = p_rel[i];
+    p_pos[i] = make_float4(x.x + (l.x + r.x), x.y + (l.y + r.y), x.z + (l.z + r.z), r.w);
 }
 
-__global__ void k_body_aabb(const float4* pos, const float4* p_rel, const int* pstart, const int* npart,
-                            float4* bmin, float4* bmax, int n) {
+__global__ void k_body_aabb(const float4* pos, const float4* pos_lo, const float4* p_rel, const int* pstart,
+                            const int* npart, float4* bmin, float4* bmax, int n) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= n) return;
     int s = pstart[b], m = npart[b];
-    float4 x = pos[b];
+    const float4 x = pos[b], xl = pos_lo[b];
     float3 lo = make_float3(INFINITY, INFINITY, INFINITY), hi = make_float3(-INFINITY, -INFINITY, -INFINITY);
     for (int k = 0; k < m; ++k) {
         float4 r = p_rel[s + k];
         float rad = fabsf(r.w);
-        // x + r -/+ rad, rounded outward at every step
-        lo.x = fminf(lo.x, __fsub_rd(__fadd_rd(x.x, r.x), rad));
-        lo.y = fminf(lo.y, __fsub_rd(__fadd_rd(x.y, r.y), rad));
-        lo.z = fminf(lo.z, __fsub_rd(__fadd_rd(x.z, r.z), rad));
-        hi.x = fmaxf(hi.x, __fadd_ru(__fadd_ru(x.x, r.x), rad));
-        hi.y = fmaxf(hi.y, __fadd_ru(__fadd_ru(x.y, r.y), rad));
-        hi.z = fmaxf(hi.z, __fadd_ru(__fadd_ru(x.z, r.z), rad));
+        // hi + (lo + r) -/+ rad, rounded outward at every step
+        lo.x = fminf(lo.x, __fsub_rd(__fadd_rd(x.x, __fadd_rd(xl.x, r.x)), rad));
+        lo.y = fminf(lo.y, __fsub_rd(__fadd_rd(x.y, __fadd_rd(xl.y, r.y)), rad));
+        lo.z = fminf(lo.z, __fsub_rd(__fadd_rd(x.z, __fadd_rd(xl.z, r.z)), rad));
+        hi.x = fmaxf(hi.x, __fadd_ru(__fadd_ru(x.x, __fadd_ru(xl.x, r.x)), rad));
+        hi.y = fmaxf(hi.y, __fadd_ru(__fadd_ru(x.y, __fadd_ru(xl.y, r.y)), rad));
+        hi.z = fmaxf(hi.z, __fadd_ru(__fadd_ru(x.z, __fadd_ru(xl.z, r.z)), rad));
     }
     if (m == 0) { lo = make_float3(0.f, 0.f, 0.f); hi = make_float3(-1.f, -1.f, -1.f); }
     bmin[b] = make_float4(lo.x, lo.y, lo.z, 0.f);
@@ -122,7 +150,8 @@ __device__ __forceinline__ void contact(const CfgParams& p, float3 n, float pen,
     f.z += ks * n.z + kt * (v.z - vn * n.z);
 }
 
-__global__ void __launch_bounds__(256) k_forces_cfg(const float4* __restrict__ pos, const float4* __restrict__ p_rel,
+__global__ void __launch_bounds__(256) k_forces_cfg(const float4* __restrict__ pos, const float4* __restrict__ pos_lo,
+                                                    const float4* __restrict__ p_rel,
                                                     const float4* __restrict__ p_vel, const int* p_body,
                                                     const int* pstart, const int* npart, const uint2* body_pairs,
                                                     const uint32_t* rowoff, uint64_t pair_cap, CfgParams p,
@@ -131,13 +160,13 @@ __global__ void __launch_bounds__(256) k_forces_cfg(const float4* __restrict__ p
     uint32_t ncontact = 0;  // particle-particle contacts of particle i (walls not counted)
     if (i < np) {
         const int a = p_body[i];
-        const float4 xa = pos[a], ri = p_rel[i], iv = p_vel[i];
+        const float4 xa = pos[a], la = pos_lo[a], ri = p_rel[i], iv = p_vel[i];
         float3 f = make_float3(0.f, 0.f, 0.f);
         float3 vw = make_float3(-iv.x, -iv.y, -iv.z);
-        const float xs[3] = {xa.x, xa.y, xa.z}, rs[3] = {ri.x, ri.y, ri.z};
+        const float xs[3] = {xa.x, xa.y, xa.z}, rs[3] = {la.x + ri.x, la.y + ri.y, la.z + ri.z};
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            // distance to the walls: (x - lo) + r and (hi - x) - r
+            // distance to the walls: (hi - wall_lo) + (lo + r) and (wall_hi - hi) - (lo + r)
             float pen_lo = ri.w - ((xs[k] - p.lo[k]) + rs[k]);
             float pen_hi = ri.w - ((p.hi[k] - xs[k]) - rs[k]);
             if (pen_lo > 0.f) {
@@ -153,8 +182,9 @@ __global__ void __launch_bounds__(256) k_forces_cfg(const float4* __restrict__ p
         if (e1 > pair_cap) e1 = (uint32_t)pair_cap;  // after an overflow (reported) rows stay in storage
         for (uint32_t e = e0; e < e1; ++e) {
             int b = (int)__ldg(&body_pairs[e].y);
-            float4 xb = __ldg(pos + b);
-            float bx = xb.x - xa.x, by = xb.y - xa.y, bz = xb.z - xa.z;
+            const float4 xb = __ldg(pos + b), lb = __ldg(pos_lo + b);
+            const float bx = (xb.x - xa.x) + (lb.x - la.x), by = (xb.y - xa.y) + (lb.y - la.y),
+                        bz = (xb.z - xa.z) + (lb.z - la.z);
             int s = __ldg(pstart + b), m = __ldg(npart + b);
             for (int l = 0; l < m; ++l) {
                 float4 rj = __ldg(p_rel + s + l);
@@ -225,9 +255,9 @@ __global__ void k_update_cfg(float4* lin, float4* ang, const float4* quat, const
 
 static inline int gr(int n) { return n <= 0 ? 1 : (n + 255) / 256; }
 
-cudaError_t rb_integrate_cfg(float4* pos, float4* quat, float4* lin, const float4* ang, const CfgParams& p, int n,
-                             cudaStream_t st) {
-    if (n > 0) k_integrate_cfg<<<gr(n), 256, 0, st>>>(pos, quat, lin, ang, p, n);
+cudaError_t rb_integrate_cfg(float4* pos, float4* pos_lo, float4* quat, float4* lin, const float4* ang,
+                             const CfgParams& p, int n, cudaStream_t st) {
+    if (n > 0) k_integrate_cfg<<<gr(n), 256, 0, st>>>(pos, pos_lo, quat, lin, ang, p, n);
     return cudaGetLastError();
 }
 cudaError_t rb_place_cfg(const float4* quat, const float4* lin, const float4* ang, const int* shape,
@@ -236,22 +266,23 @@ cudaError_t rb_place_cfg(const float4* quat, const float4* lin, const float4* an
     if (np > 0) k_place_cfg<<<gr(np), 256, 0, st>>>(quat, lin, ang, shape, pstart, p_body, ref_pos, p_rel, p_vel, np);
     return cudaGetLastError();
 }
-cudaError_t rb_abs_pos(const float4* pos, const int* p_body, const float4* p_rel, float4* p_pos, int np,
-                       cudaStream_t st) {
-    if (np > 0) k_abs_pos<<<gr(np), 256, 0, st>>>(pos, p_body, p_rel, p_pos, np);
+cudaError_t rb_abs_pos(const float4* pos, const float4* pos_lo, const int* p_body, const float4* p_rel, float4* p_pos,
+                       int np, cudaStream_t st) {
+    if (np > 0) k_abs_pos<<<gr(np), 256, 0, st>>>(pos, pos_lo, p_body, p_rel, p_pos, np);
     return cudaGetLastError();
 }
-cudaError_t rb_body_aabb(const float4* pos, const float4* p_rel, const int* pstart, const int* npart, float4* bmin,
-                         float4* bmax, int n, cudaStream_t st) {
-    if (n > 0) k_body_aabb<<<gr(n), 256, 0, st>>>(pos, p_rel, pstart, npart, bmin, bmax, n);
+cudaError_t rb_body_aabb(const float4* pos, const float4* pos_lo, const float4* p_rel, const int* pstart,
+                         const int* npart, float4* bmin, float4* bmax, int n, cudaStream_t st) {
+    if (n > 0) k_body_aabb<<<gr(n), 256, 0, st>>>(pos, pos_lo, p_rel, pstart, npart, bmin, bmax, n);
     return cudaGetLastError();
 }
-cudaError_t rb_forces_cfg(const float4* pos, const float4* p_rel, const float4* p_vel, const int* p_body,
-                          const int* pstart, const int* npart, const uint2* body_pairs, const uint32_t* rowoff,
-                          uint64_t pair_cap, const CfgParams& p, float4* p_force, int np, cudaStream_t st) {
+cudaError_t rb_forces_cfg(const float4* pos, const float4* pos_lo, const float4* p_rel, const float4* p_vel,
+                          const int* p_body, const int* pstart, const int* npart, const uint2* body_pairs,
+                          const uint32_t* rowoff, uint64_t pair_cap, const CfgParams& p, float4* p_force, int np,
+                          cudaStream_t st) {
     if (np > 0)
-        k_forces_cfg<<<gr(np), 256, 0, st>>>(pos, p_rel, p_vel, p_body, pstart, npart, body_pairs, rowoff, pair_cap, p,
-                                             p_force, np);
+        k_forces_cfg<<<gr(np), 256, 0, st>>>(pos, pos_lo, p_rel, p_vel, p_body, pstart, npart, body_pairs, rowoff,
+                                             pair_cap, p, p_force, np);
     return cudaGetLastError();
 }
 cudaError_t rb_update_cfg(float4* lin, float4* ang, const float4* quat, const float* inv_mass, const int* shape,

@@ -174,16 +174,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_onesweep(BpScratch S, const uin
                 // flags (set by the projection): a pair is owned by the cell
                 // of (max lo2, max lo3), which both objects touch, so the
                 // cell owns it iff each coordinate is some member's lowest.
-                const uint32_t obj = vv & kObjMask, fl = vv >> kFlagShift;
-                const float4 lo = __ldg(G.mn + obj);
-                if (G.mx) {  // boxes: index and flags ride in the unused w lanes
-                    const float4 hi = __ldg(G.mx + obj);
-                    G.smin[g] = make_float4(lo.x, lo.y, lo.z, __uint_as_float(obj));
-                    G.smax[g] = make_float4(hi.x, hi.y, hi.z, __uint_as_float(fl));
-                } else {     // spheres: radius in w, index and flags in the second record
-                    G.smin[g] = lo;
-                    G.smax[g] = make_float4(__uint_as_float(obj), __uint_as_float(fl), 0.f, 0.f);
-                }
+                put_record(S, G, g, kk, vv);
             }
         }
         __syncthreads();  // s_k / s_v / s_wh / s_next are reused by the next tile

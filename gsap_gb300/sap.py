@@ -82,13 +82,14 @@ class Sap:
 
     def __init__(self, max_n: int, mode: int = MODE_AABB, axis_mode: int = AXIS_PCA, max_scenes: int = 1,
                  entry_factor: int = 8, pair_factor: int = 16, sort_bits: int = 32, cell_factor: float = 2.0,
-                 spin_limit: int = 0):
+                 spin_limit: int = 0, sort_mode: int = 0):
         L = load()
         cfg = Config()
         L.gsap_config_default(C.byref(cfg))
         cfg.mode, cfg.axis_mode, cfg.max_scenes = mode, axis_mode, max_scenes
         cfg.entry_factor, cfg.pair_factor, cfg.sort_bits = entry_factor, pair_factor, sort_bits
         cfg.cell_factor = cell_factor
+        cfg.sort_mode = sort_mode
         if spin_limit:
             cfg.spin_limit = spin_limit
         self.cfg = cfg
@@ -162,9 +163,9 @@ class Sap:
     def autotune(self, mn: torch.Tensor, mx: torch.Tensor | None = None, offsets: torch.Tensor | None = None,
                  pairs: torch.Tensor | None = None, sorted: bool = True, graph: bool = True, reps: int = 3,
                  stream=None) -> dict:
-        """Picks key width and cell factor for this kind of input by timing a
-        small grid on it (gsap_sap_autotune); the handle keeps the fastest.
-        Returns the chosen settings."""
+        """Picks the sort (bucket or radix), key width and cell factor for
+        this kind of input by timing a small grid on it (gsap_sap_autotune);
+        the handle keeps the fastest.  Returns the chosen settings."""
         n = mn.shape[0]
         _dev_ptr(mn, "mn", torch.float32, 4)
         _dev_ptr(mx, "mx", torch.float32, 4)
@@ -179,7 +180,8 @@ class Sap:
                                        C.c_uint32(n), pairs.data_ptr(), C.c_uint64(pairs.shape[0]),
                                        C.c_uint32(flags), C.c_int(reps), C.byref(cfg),
                                        C.c_void_p(_stream_ptr(stream))))
-        return {"sort_bits": int(cfg.sort_bits), "cell_factor": float(cfg.cell_factor)}
+        return {"sort_bits": int(cfg.sort_bits), "cell_factor": float(cfg.cell_factor),
+                "sort": "radix" if cfg.sort_mode == 0 else "bucket"}
 
     def broadphase_async(self, mn, mx, pairs, d_count, sorted=False, graph=False, temporal=False, stream=None):
         """Asynchronous form: the pair count goes to the device tensor

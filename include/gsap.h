@@ -33,7 +33,7 @@ extern "C" {
 #endif
 
 #define GSAP_VERSION_MAJOR 1
-#define GSAP_VERSION_MINOR 0
+#define GSAP_VERSION_MINOR 1
 
 /* Error handling replaces cutilSafeCall aborts (Sap.cpp:65-86) and the
  * printf-and-return-0 overflow path (SapKernel.cu:2417, :2496). */
@@ -82,7 +82,14 @@ typedef struct gsap_config {
     uint32_t sort_bits;     /* radix key width, 24 or 32 (0 -> 32) */
     float cell_factor;      /* cell size / mean projected width on the secondary axes (0 -> 2.0) */
     uint32_t spin_limit;    /* iteration cap of every device-side wait (0 -> default) */
+    uint32_t sort_mode;     /* GSAP_SORT_* : how the sweep entries are sorted (0 -> radix) */
 } gsap_config;
+
+/* Sort of the sweep entries (the pair set is the same either way). */
+enum {
+    GSAP_SORT_RADIX = 0,  /* LSD onesweep radix passes over all entries */
+    GSAP_SORT_BUCKET = 1  /* counting scatter into sub-buckets, then a shared-memory sort of each */
+};
 
 /* Fills *cfg with the defaults. */
 void gsap_config_default(gsap_config* cfg);

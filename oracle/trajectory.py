@@ -92,7 +92,8 @@ def fp64_errors(prb, sap, sc: dict, params: dict, steps: int = 100, check_scenes
     per = {"pos": [], "lin_vel": [], "ang_vel": []}
     per_all = {"pos": [], "lin_vel": [], "ang_vel": []}
     left_out = []
-    for _ in range(steps):
+    worst = {}
+    for step in range(steps):
         cur = prb.get_state()
         for k in KEYS:
             r = st_sync[k].astype(np.float32)
@@ -106,13 +107,21 @@ def fp64_errors(prb, sap, sc: dict, params: dict, steps: int = 100, check_scenes
         keep = amb == 0
         left_out.append(int(nb - keep.sum()))
         for k in per:
-            per[k].append(_rel(got[k][:nb], st_sync[k], keep))
+            e = _rel(got[k][:nb], st_sync[k], keep)
+            per[k].append(e)
             per_all[k].append(_rel(got[k][:nb], st_sync[k]))
+            if e >= max(per[k]):
+                d = np.abs(np.asarray(got[k][:nb], np.float64)[:, :3] - st_sync[k][:, :3]).max(1)
+                d[~keep] = 0.0
+                b = int(np.argmax(d))
+                worst[k] = {"step": step, "body": b, "abs_err": float(d[b]),
+                            "max_abs_ref": float(np.abs(st_sync[k][:, :3]).max()),
+                            "body_abs_ref": float(np.abs(st_sync[k][b, :3]).max())}
     st64 = st_true
     sap.check()
     return {"steps": steps, "checked_bodies": nb, "onset_band": band,
             "per_step_max": {k: max(v) for k, v in per.items()},
             "per_step_max_all_bodies": {k: max(v) for k, v in per_all.items()},
             "bodies_left_out_max": max(left_out), "bodies_left_out_mean": float(np.mean(left_out)),
-            "per_step": per,
+            "per_step": per, "worst": worst,
             "free_running": {k: _rel(free[k][:nb], st64[k]) for k in ("pos", "lin_vel", "ang_vel")}}

@@ -294,19 +294,44 @@ def test_autotune_keeps_the_pair_set(cuda, oracle_lib):
         assert np.array_equal(sub, oracle_lib.bf_aabb(mnb[a:b], mxb[a:b])), s
 
 
+@pytest.mark.parametrize("sort_mode", [0, 1])
 @pytest.mark.parametrize("sort_bits", [24, 32])
 @pytest.mark.parametrize("cell_factor", [0.5, 1.0, 2.0, 4.0])
-def test_every_setting_gives_the_same_pairs(cuda, oracle_lib, sort_bits, cell_factor):
-    """Key width and cell size only move work between stages: the pair set
-    is the brute force's for every setting the autotuner may pick."""
+def test_every_setting_gives_the_same_pairs(cuda, oracle_lib, sort_bits, cell_factor, sort_mode):
+    """Sort (bucket or radix), key width and cell size only move work
+    between stages: the pair set is the brute force's for every setting the
+    autotuner may pick."""
     from gsap_gb300 import Sap, scenes
     n = 30_000
     c, h, _ = scenes.aabb_gauss_parts(n, seed=21, std=(25.0, 6.0, 2.0))
     mn = np.concatenate([c - h, np.zeros((n, 1), np.float32)], 1)
     mx = np.concatenate([c + h, np.zeros((n, 1), np.float32)], 1)
-    sap = Sap(n, sort_bits=sort_bits, cell_factor=cell_factor)
+    sap = Sap(n, sort_bits=sort_bits, cell_factor=cell_factor, sort_mode=sort_mode)
     assert np.array_equal(run_bp(sap, mn, mx, cuda), oracle_lib.bf_aabb(mn, mx))
     assert np.array_equal(run_bp(sap, mn, mx, cuda, sorted=False), oracle_lib.bf_aabb(mn, mx))
+
+
+@pytest.mark.parametrize("sort_bits", [24, 32])
+def test_bucket_sort_sub_bucket_larger_than_shared_memory(cuda, oracle_lib, sort_bits):
+    """A dense line of 20,000 thin boxes inside one cell, stretched out by a
+    few far outliers so that one sub-bucket holds far more entries than a
+    CTA sorts in shared memory: the bucket sort takes its global-memory path
+    and the pair set is still the brute force's (the radix path agrees)."""
+    from gsap_gb300 import Sap
+    rng = np.random.default_rng(31)
+    m = 20_000
+    c = np.stack([rng.uniform(0, 10, m), rng.uniform(0, 1, m), rng.uniform(0, 1, m)], 1)
+    h = np.stack([np.full(m, 0.001), np.full(m, 0.5), np.full(m, 0.5)], 1)
+    far = np.array([[1000.0, 0.5, 0.5], [-1000.0, 0.5, 0.5], [900.0, 0.4, 0.6], [-900.0, 0.6, 0.4]])
+    c = np.concatenate([c, far]).astype(np.float32)
+    h = np.concatenate([h, np.full((4, 3), 0.5)]).astype(np.float32)
+    n = len(c)
+    mn = np.concatenate([c - h, np.zeros((n, 1), np.float32)], 1)
+    mx = np.concatenate([c + h, np.zeros((n, 1), np.float32)], 1)
+    want = oracle_lib.bf_aabb(mn, mx)
+    for sort_mode in (0, 1):
+        sap = Sap(n, sort_bits=sort_bits, sort_mode=sort_mode)
+        assert np.array_equal(run_bp(sap, mn, mx, cuda), want), sort_mode
 
 
 def test_batched_with_empty_and_tiny_scenes(cuda, oracle_lib):

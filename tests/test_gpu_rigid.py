@@ -173,6 +173,7 @@ def check_fp64_errors(e, nb):
           "free-running", e["free_running"])
     assert e["per_step_max"]["pos"] <= REL_TOL
     assert e["per_step_max"]["lin_vel"] <= REL_TOL
+    assert e["per_step_max"]["ang_vel"] <= REL_TOL
     assert e["bodies_left_out_max"] <= LEFT_OUT_SHARE * nb
     for k, tol in FREE_RUN_TOL.items():
         assert e["free_running"][k] <= tol, (k, e["free_running"][k])
