@@ -200,14 +200,15 @@ def run_ours(args, world, rank, local):
     host_sets, R = make_inputs(rank, n, args.jitter_sets)
     dsets = [(torch.from_numpy(mn).to(dev), torch.from_numpy(mx).to(dev)) for mn, mx in host_sets]
     fixed = (args.cell_factor is not None or args.sort_bits is not None or args.sort is not None
-             or args.no_tune)
+             or args.sort_tile is not None or args.no_tune)
     sort_mode = {"radix": 0, "bucket": 1}[args.sort or "radix"]
-    sap = Sap(n, cell_factor=args.cell_factor or 2.0, sort_bits=args.sort_bits or 32, sort_mode=sort_mode)
+    sap = Sap(n, cell_factor=args.cell_factor or 2.0, sort_bits=args.sort_bits or 32, sort_mode=sort_mode,
+              sort_tile=args.sort_tile or 4096)
     cap = 16 * n
     pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
     d_count = torch.zeros(1, dtype=torch.int64, device=dev)
     stream = torch.cuda.current_stream()
-    # autotuner (set-up, untimed): sort, key width and cell factor for this input
+    # autotuner (set-up, untimed): sort (and radix tile), key width and cell factor for this input
     tuned = None if fixed else sap.autotune(*dsets[0], pairs=pairs, sorted=True, graph=True, reps=10, stream=stream)
     passes = (tuned["sort_bits"] if tuned else (args.sort_bits or 32)) // 8
     if tuned:
@@ -427,7 +428,7 @@ def run_ours(args, world, rank, local):
         "pairs_per_call": P0,
         "settings": dict(tuned, autotuned=True) if tuned else
         {"sort_bits": args.sort_bits or 32, "cell_factor": args.cell_factor or 2.0, "sort": args.sort or "radix",
-         "autotuned": False},
+         "sort_tile": args.sort_tile or 4096, "autotuned": False},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": f"stage:{dom}",
                      "peak_kind": peak_kind,
@@ -610,7 +611,7 @@ def _extra_batched(args, dev, stream, out):
     n = len(mn)
     dmn, dmx = torch.from_numpy(mn).to(dev), torch.from_numpy(mx).to(dev)
     doff = torch.from_numpy(off.astype(np.int32)).to(dev)
-    bsap = Sap(n, max_scenes=S, pair_factor=2)
+    bsap = Sap(n, max_scenes=S, pair_factor=2, sort_tile=args.sort_tile or 0)
     cap = 2 * n
     pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
     cnt = torch.zeros(1, dtype=torch.int64, device=dev)
@@ -618,7 +619,8 @@ def _extra_batched(args, dev, stream, out):
 
     from gsap_gb300 import _lib
     L = _lib.load()
-    btuned = (dict(sort_bits=32, cell_factor=2.0, sort="radix", autotuned=False) if args.no_tune else
+    btuned = (dict(sort_bits=32, cell_factor=2.0, sort="radix", sort_tile=args.sort_tile or 4096, autotuned=False)
+              if args.no_tune else
               dict(bsap.autotune(dmn, dmx, offsets=doff, pairs=pairs, sorted=True, graph=True, reps=3, stream=stream),
                    autotuned=True))
 
@@ -966,6 +968,8 @@ def main():
     ap.add_argument("--sort-bits", type=int, default=None, choices=[24, 32], help="radix key width (default: autotuned)")
     ap.add_argument("--sort", default=None, choices=["bucket", "radix"],
                     help="how the sweep entries are sorted (default: autotuned)")
+    ap.add_argument("--sort-tile", type=int, default=None, choices=[2048, 4096],
+                    help="keys per radix tile (default: autotuned)")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (defaults: 32 bits, cell factor 2.0)")
     ap.add_argument("--jitter-sets", type=int, default=N_JITTER,
                     help="distinct jittered inputs cycled by the timed calls (64 = the workload)")

@@ -31,7 +31,8 @@ class GsapError(RuntimeError):
 class Config(C.Structure):
     _fields_ = [("mode", C.c_uint32), ("axis_mode", C.c_uint32), ("max_scenes", C.c_uint32),
                 ("entry_factor", C.c_uint32), ("pair_factor", C.c_uint32), ("sort_bits", C.c_uint32),
-                ("cell_factor", C.c_float), ("spin_limit", C.c_uint32), ("sort_mode", C.c_uint32)]
+                ("cell_factor", C.c_float), ("spin_limit", C.c_uint32), ("sort_mode", C.c_uint32),
+                ("sort_tile", C.c_uint32)]
 
 
 class BodyData(C.Structure):

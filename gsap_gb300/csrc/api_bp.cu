@@ -75,6 +75,7 @@ extern "C" void gsap_config_default(gsap_config* c) {
     c->sort_bits = 32;
     c->cell_factor = 2.0f;
     c->spin_limit = kDefaultSpin;
+    c->sort_tile = kSortTile;
 }
 
 // ------------------------------------------------------------------ handle
@@ -88,7 +89,7 @@ struct GraphShape {
     uint32_t n, S, flags, mode, both;
     uint32_t key_bits;
     float cell_factor;
-    uint32_t sort_mode;
+    uint32_t sort_mode, sort_tile;
     uint64_t cap, ecap;
     bool operator==(const GraphShape& o) const { return memcmp(this, &o, sizeof(*this)) == 0; }
 };
@@ -164,6 +165,11 @@ extern "C" gsap_sap* gsap_sap_create(uint32_t max_n, const gsap_config* cfg) {
         fail(GSAP_ERR_INVALID, "unknown sort_mode %u", c.sort_mode);
         return nullptr;
     }
+    if (c.sort_tile == 0) c.sort_tile = kSortTile;
+    if (c.sort_tile != (uint32_t)kSortTile && c.sort_tile != (uint32_t)kSortTileMin) {
+        fail(GSAP_ERR_INVALID, "sort_tile must be %d or %d", kSortTileMin, kSortTile);
+        return nullptr;
+    }
     if (max_n == 0) max_n = 1;
     uint64_t ecap = (uint64_t)c.entry_factor * max_n + 4096;
     if (ecap >= (1ull << 30)) { fail(GSAP_ERR_INVALID, "entry capacity %llu exceeds 2^30", (unsigned long long)ecap); return nullptr; }
@@ -179,7 +185,7 @@ extern "C" gsap_sap* gsap_sap_create(uint32_t max_n, const gsap_config* cfg) {
     s.max_work = (max_n + kChunk - 1) / kChunk + c.max_scenes + 1;
     s.entry_cap = ecap;
     s.pair_cap_internal = (uint64_t)c.pair_factor * max_n + 4096;
-    uint64_t tiles = (ecap + kSortTile - 1) / kSortTile + 1;
+    uint64_t tiles = (ecap + kSortTileMin - 1) / kSortTileMin + 1;  // status words for the smaller tile
     s.status_words = tiles * 256 + (max_n / 2048 + 2);  // digit words, scan words
     bool ok = true;
     auto A = [&](void** p, size_t bytes) {
@@ -339,7 +345,7 @@ static gsap_status record(gsap_sap* h, const Call& c, cudaStream_t st, bool time
             const bool last = p == passes - 1;
             CK(launch_sort_pass(s, p, passes, s.keys[src], s.vals[src], s.keys[src ^ 1],
                                 last ? nullptr : s.vals[src ^ 1], count, s.entry_cap, a.spin_limit, st,
-                                last ? &gather : nullptr, true));
+                                last ? &gather : nullptr, true, 0, (int)h->cfg.sort_tile));
             src ^= 1;
         }
     }
@@ -377,6 +383,7 @@ static gsap_status run(gsap_sap* h, const Call& c, cudaStream_t st) {
     sh.cap = c.cap; sh.ecap = c.ecap;
     sh.key_bits = h->cfg.sort_bits; sh.cell_factor = h->cfg.cell_factor;  // tuned settings are baked into a graph
     sh.sort_mode = h->cfg.sort_mode;
+    sh.sort_tile = h->cfg.sort_tile;
     // LRU cache of captured pipelines, one per (inputs, outputs, sizes, flags)
     GraphEntry* hit = nullptr;
     size_t same = 0;
@@ -517,7 +524,10 @@ extern "C" gsap_status gsap_broadphase_aabb(gsap_sap* h, const float* d_min, con
 
 // Times every (sort, key width, cell factor) setting of a small grid on the
 // caller's input and keeps the fastest in the handle.  The sort is the
-// bucket sort or the onesweep radix passes; the key width sets the radix
+// bucket sort or the onesweep radix passes with 4096- or 2048-key tiles
+// (more, shorter tiles: a longer look-back chain but more CTAs per SM); the
+// digit width stays 8 bits (11-bit digits would multiply the look-back
+// words and the per-tile digit counters by 8).  The key width sets the radix
 // passes (24 bits: three 8-bit digits, 32 bits: four) and the q resolution
 // of the sweep; the cell factor sets the cell edge on u2/u3 and with it the
 // replication (entries to sort) against the candidate run length (tests).
@@ -530,7 +540,10 @@ extern "C" gsap_status gsap_sap_autotune(gsap_sap* h, const float* d_min, const 
     if (reps < 1) reps = 1;
     if (d_scene_offsets && num_scenes == 0) return fail(GSAP_ERR_INVALID, "batched call needs scene offsets");
     const uint32_t S = d_scene_offsets ? num_scenes : 1;
-    const uint32_t sort_grid[2] = {GSAP_SORT_RADIX, GSAP_SORT_BUCKET};
+    // (sort, radix tile): the bucket sort has no tile setting
+    const uint32_t sort_grid[3][2] = {{GSAP_SORT_RADIX, (uint32_t)kSortTile},
+                                      {GSAP_SORT_RADIX, (uint32_t)kSortTileMin},
+                                      {GSAP_SORT_BUCKET, (uint32_t)kSortTile}};
     const uint32_t bits_grid[2] = {24, 32};
     const float cf_grid[5] = {1.0f, 1.5f, 2.0f, 2.5f, 3.0f};
     const gsap_config saved = h->cfg;
@@ -540,10 +553,11 @@ extern "C" gsap_status gsap_sap_autotune(gsap_sap* h, const float* d_min, const 
     CK(cudaEventCreate(&e1));
     float best_ms = -1.f;
     gsap_config best = saved;
-    for (uint32_t sm : sort_grid)
+    for (const auto& sm : sort_grid)
         for (uint32_t bits : bits_grid)
             for (float cf : cf_grid) {
-                h->cfg.sort_mode = sm;
+                h->cfg.sort_mode = sm[0];
+                h->cfg.sort_tile = sm[1];
                 h->cfg.sort_bits = bits;
                 h->cfg.cell_factor = cf;
                 uint64_t cnt = 0;

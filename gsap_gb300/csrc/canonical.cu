@@ -229,9 +229,19 @@ __global__ void __launch_bounds__(1024) k_tilescan(uint32_t* tsum, uint32_t ntil
     }
 }
 
+// Who puts the row counters back to zero for the next call: the row scan
+// (a sequential write of all n counters) when pairs are many, k_scatter
+// (one write per stored pair, to rows it touches anyway) when they are few
+// against the rows -- e.g. 0.8M pairs over 38.6M objects in a batch of
+// scenes, where zeroing every counter would be a third of the scan's bytes.
+// Both kernels decide from the same stored pair count.
+__device__ __forceinline__ bool scatter_zeroes(uint64_t pairs, uint32_t n) { return pairs * 4ull < n; }
+
 // scanned != 0: tsum holds every tile's exclusive offset (k_tilescan ran).
 __global__ void __launch_bounds__(kThreads) k_rowscan(uint32_t* in, uint32_t* out, const uint32_t* __restrict__ tsum,
-                                                      uint32_t n, int scanned) {
+                                                      uint32_t n, int scanned, const Ctrl* __restrict__ C,
+                                                      uint64_t pair_cap) {
+    const bool zero = !scatter_zeroes(min((uint64_t)C->pair_count, pair_cap), n);
     __shared__ uint32_t s_w[kThreads / 32];
     const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const uint32_t t = blockIdx.x;
@@ -253,14 +263,14 @@ __global__ void __launch_bounds__(kThreads) k_rowscan(uint32_t* in, uint32_t* ou
         for (int q = 0; q < kScanItems / 4; ++q) {
             const uint4 x4 = src[q];
             v[4 * q] = x4.x; v[4 * q + 1] = x4.y; v[4 * q + 2] = x4.z; v[4 * q + 3] = x4.w;
-            src[q] = make_uint4(0u, 0u, 0u, 0u);
+            if (zero) src[q] = make_uint4(0u, 0u, 0u, 0u);
         }
     } else {
 #pragma unroll
         for (int k = 0; k < kScanItems; ++k) {
             const uint32_t i = b + k;
             v[k] = i < n ? in[i] : 0u;
-            if (i < n) in[i] = 0u;
+            if (i < n && zero) in[i] = 0u;
         }
     }
     uint32_t sum = 0;
@@ -303,10 +313,13 @@ __global__ void __launch_bounds__(kThreads) k_rowscan(uint32_t* in, uint32_t* ou
 }
 
 // Scatter pairs into their rows at the slots the sweep drew.  both: row i
-// gets (i, j) and row j (j, i).  No atomics.
+// gets (i, j) and row j (j, i).  No atomics.  With few pairs against the
+// rows (scatter_zeroes) it also puts the counters of the rows it touches
+// back to zero; the other rows' counters are zero already.
 __global__ void __launch_bounds__(kThreads) k_scatter(BpScratch S, const uint2* __restrict__ in, uint64_t in_cap,
-                                                      uint2* out, uint64_t out_cap, int both) {
+                                                      uint2* out, uint64_t out_cap, int both, uint32_t n) {
     const uint64_t P = min((uint64_t)S.ctrl->pair_count, in_cap);
+    const bool zero = scatter_zeroes(P, n);
     const uint32_t* off = S.rowoff;
     const uint32_t* __restrict__ rank1 = S.tmp_rank;
     const uint2* __restrict__ rank2 = reinterpret_cast<const uint2*>(S.tmp_rank);
@@ -321,6 +334,14 @@ __global__ void __launch_bounds__(kThreads) k_scatter(BpScratch S, const uint2* 
             if (k < P) {
                 p[u] = in[k];
                 r[u] = both ? rank2[k] : make_uint2(rank1[k], 0u);
+            }
+        }
+        if (zero) {
+#pragma unroll
+            for (int u = 0; u < kPer; ++u) {
+                if (k0 + u * stride >= P) continue;
+                S.rowcnt[p[u].x] = 0u;
+                if (both) S.rowcnt[p[u].y] = 0u;
             }
         }
 #pragma unroll
@@ -436,9 +457,9 @@ cudaError_t launch_canonical(const BpScratch& s, uint32_t n, const uint2* in_pai
     k_rowsum<<<ntiles, kThreads, 0, st>>>(s.rowcnt, s.tile_sums, n);
     const int scanned = ntiles > kDirectTiles ? 1 : 0;
     if (scanned) k_tilescan<<<1, 1024, 0, st>>>(s.tile_sums, ntiles);
-    k_rowscan<<<ntiles, kThreads, 0, st>>>(s.rowcnt, s.rowoff, s.tile_sums, n, scanned);
+    k_rowscan<<<ntiles, kThreads, 0, st>>>(s.rowcnt, s.rowoff, s.tile_sums, n, scanned, s.ctrl, in_cap);
     const uint64_t grp_cap = 2 * s.pair_cap_internal;
-    k_scatter<<<sm_count() * 16, kThreads, 0, st>>>(s, in_pairs, in_cap, s.grp_pairs, grp_cap, both);
+    k_scatter<<<sm_count() * 16, kThreads, 0, st>>>(s, in_pairs, in_cap, s.grp_pairs, grp_cap, both, n);
     k_rank<<<sm_count() * 8, kThreads, 0, st>>>(s, s.grp_pairs, grp_cap, n, out_pairs, out_cap);
     k_rowsort_long<<<sm_count() * 2, kThreads, 0, st>>>(s, s.grp_pairs, out_pairs, out_cap);
     if (both && entries) k_scan<1><<<grid, kThreads, 0, st>>>(s, s.rowoff, nullptr, entries, entry_cap, n, 6, spin);

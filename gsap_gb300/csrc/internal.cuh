@@ -23,8 +23,10 @@ int per_device(std::once_flag (&once)[kMaxDevices], int (&val)[kMaxDevices], F c
 constexpr int kChunk = 4096;          // objects per PCA / projection work item
 constexpr int kThreads = 256;         // threads per CTA of the streaming kernels
 constexpr int kMaxPasses = 4;         // radix passes (8-bit digits, <= 32-bit keys)
-constexpr int kSortItems = 16;        // keys per thread in a onesweep tile
+constexpr int kSortItems = 16;        // keys per thread in a onesweep tile (default)
 constexpr int kSortTile = kThreads * kSortItems;
+constexpr int kSortItemsSmall = 8;    // the smaller tile the autotuner may choose
+constexpr int kSortTileMin = kThreads * kSortItemsSmall;
 constexpr uint32_t kDefaultSpin = 1u << 24;
 // Bucket sort: a sub-bucket is a cell together with the top T bits of the
 // quantised lower bound, i.e. the top bits of the key above `shift`; at most
@@ -187,10 +189,13 @@ struct SortGather {
 // image as they are loaded (first pass of a float sort), kSortUnflipOut maps
 // them back as they are stored (last pass).
 enum : int { kSortFlipIn = 1, kSortUnflipOut = 2 };
+// tile: keys per tile, kSortTile or kSortTileMin (the status table must
+// hold 256 words per tile of that size).
 cudaError_t launch_sort_pass(const BpScratch& s, int pass, int passes, const uint32_t* kin,
                              const uint32_t* vin, uint32_t* kout, uint32_t* vout,
                              const uint32_t* count_ptr, uint64_t cap, uint32_t spin, cudaStream_t st,
-                             const SortGather* gather = nullptr, bool count_next = false, int fmode = 0);
+                             const SortGather* gather = nullptr, bool count_next = false, int fmode = 0,
+                             int tile = kSortTile);
 // Counter reset and the digit histograms of a standalone sort (flip != 0:
 // of the float images of the keys).
 cudaError_t launch_sort_prep(const BpScratch& s, const uint32_t* keys, const uint32_t* count_ptr,

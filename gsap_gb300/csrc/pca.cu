@@ -6,14 +6,14 @@
 // tree reductions over float4 arrays (the covariance rows pre-divided by n
 // and written to two 16n-byte temporaries) feed a <<<1,1>>> kernel that picks
 // the coordinate axis of largest variance.  Here one pass over the input
-// (k_pca) accumulates per 4096-object work item compensated (two-sum) FP32
-// sums of d = c - pilot and d d^T, and plain FP32 sums of the half extents h
-// and h h^T (they only size the grid); then one CTA per scene (k_pca_finish)
-// combines its partials in float-float arithmetic in a fixed order
-// (deterministic), forms the covariance in FP64, solves the 3x3 eigenproblem
-// (FP32 Jacobi refined in FP64, scene_math.cuh) and chooses the sweep grid;
-// the last scene lays out the keys and resets the counters of the later
-// stages.
+// (k_pca) accumulates per 4096-object work item FP32 sums of d = c - pilot
+// and d d^T (per thread plain, merged as compensated two-sum pairs), and of
+// the half extents h and h h^T (they only size the grid); then one CTA per
+// scene (k_pca_finish; k_pca_finish_batch for batches) combines its partials
+// in float-float arithmetic in a fixed order (deterministic), forms the
+// covariance in FP64, solves the 3x3 eigenproblem (FP32 Jacobi,
+// scene_math.cuh) and chooses the sweep grid; the last scene lays out the
+// keys and resets the counters of the later stages.
 #include "internal.cuh"
 #include "scene_math.cuh"
 #include <math.h>
@@ -90,8 +90,12 @@ __global__ void __launch_bounds__(kThreads) k_pca(BpScratch S, BpArgs A) {
     // pilot = centre of the scene's first object (shift against cancellation)
     float px = 0.f, py = 0.f, pz = 0.f;
     pilot_of(A, sb, se, px, py, pz);
-    // Covariance sums (d, d d^T) are compensated (two-sum); the extent sums
-    // (h, h h^T) only size the grid and are plain FP32 (lo stays 0).
+    // Each thread sums its (at most kChunk / kThreads = 16) objects in plain
+    // FP32: d is taken about the pilot, so its terms are of the scene's
+    // spread and 16 of them lose at most ~16 ulps.  From there on the sums
+    // are compensated: the warp, CTA and cross-CTA merges carry (hi, lo)
+    // pairs.  (Compensating every object's terms cost ~120 FP32 operations
+    // per object and made the kernel issue-bound on large batches.)
     float hi[kPcaQ], lo[kPcaQ], hm[3] = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int q = 0; q < kPcaQ; ++q) { hi[q] = 0.f; lo[q] = 0.f; }
@@ -126,7 +130,7 @@ __global__ void __launch_bounds__(kThreads) k_pca(BpScratch S, BpArgs A) {
             float dx = cx - px, dy = cy - py, dz = cz - pz;
             const float v[9] = {dx, dy, dz, dx * dx, dx * dy, dx * dz, dy * dy, dy * dz, dz * dz};
 #pragma unroll
-            for (int q = 0; q < 9; ++q) kahan_add(hi[q], lo[q], v[q]);
+            for (int q = 0; q < 9; ++q) hi[q] += v[q];
             const float w[9] = {hx, hy, hz, hx * hx, hx * hy, hx * hz, hy * hy, hy * hz, hz * hz};
 #pragma unroll
             for (int q = 0; q < 9; ++q) hi[9 + q] += w[q];
@@ -365,11 +369,10 @@ __global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, 
 // kFinishScenes consecutive scenes: each of its warps merges the partials of
 // some of them (lane l merges items l, l+32, ... in float-float, then a fixed
 // shuffle tree, so the result does not depend on timing), and warp 0 then
-// solves all of them side by side, one scene per lane.  GB300 issues an FP64
-// warp instruction at a small fraction of the FP32 rate however few of its
-// lanes are active, so solving 32 scenes per warp instruction rather than
-// one cuts the FP64 time of a batch about 32-fold.  The last CTA to finish
-// lays out the keys and resets the counters, as k_pca_finish does.
+// solves all of them side by side, one scene per lane, instead of one lane
+// of a warp (or one thread of a CTA) per scene: a batch's serial solves then
+// share warp instructions.  The last CTA to finish lays out the keys and
+// resets the counters, as k_pca_finish does.
 constexpr int kFinishWarps = 16;
 constexpr int kFinishScenes = 32;
 __global__ void __launch_bounds__(32 * kFinishWarps) k_pca_finish_batch(BpScratch S, BpArgs A, uint64_t entry_cap,
@@ -425,37 +428,54 @@ __global__ void __launch_bounds__(32 * kFinishWarps) k_pca_finish_batch(BpScratc
         }
     }
     __syncthreads();
-    if (wid != 0) return;
-    const uint32_t cnt = min((uint32_t)kFinishScenes, A.num_scenes - s0);
-    if (lane < cnt) {
-        Scene sc;
-        choose_scene(s_z[lane], A, entry_cap, A.n, sc);
-        out[s0 + lane] = sc;
-    }
-    __threadfence();
-    __syncwarp();
-    uint32_t last = 0;
-    if (lane == 0) last = atomicAdd(&C->scenes_done, cnt) + cnt == A.num_scenes ? 1u : 0u;
-    last = __shfl_sync(0xffffffffu, last, 0);
-    if (!last) return;
-    __threadfence();  // the other scenes' records are read below
-    // Last scene: global bucket bases, key layout, counter reset.
-    uint32_t carry = 0;
-    for (uint32_t base = 0; base < A.num_scenes; base += 32) {
-        const uint32_t s = base + lane;
-        const uint32_t v = s < A.num_scenes ? __ldcg(&out[s].G2) * __ldcg(&out[s].G3) : 0u;
-        uint32_t x = v;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= (uint32_t)o) x += y;
+    __shared__ uint32_t s_last;
+    if (wid == 0) {
+        const uint32_t cnt = min((uint32_t)kFinishScenes, A.num_scenes - s0);
+        if (lane < cnt) {
+            Scene sc;
+            choose_scene(s_z[lane], A, entry_cap, A.n, sc);
+            out[s0 + lane] = sc;
         }
-        if (s < A.num_scenes) out[s].bucket_base = carry + x - v;
-        carry += __shfl_sync(0xffffffffu, x, 31);
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) s_last = atomicAdd(&C->scenes_done, cnt) + cnt == A.num_scenes ? 1u : 0u;
     }
-    const uint32_t total = carry;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();  // the other scenes' records are read below
+    // Last CTA: global bucket bases (an exclusive scan of G2 * G3 over the
+    // scenes, each thread a contiguous chunk whose loads are issued
+    // together), key layout, counter reset, quantisation scales.
+    constexpr uint32_t kT = 32 * kFinishWarps;
+    const uint32_t tid = threadIdx.x;
+    const uint32_t per = (A.num_scenes + kT - 1) / kT;
+    const uint32_t c0 = min(tid * per, A.num_scenes), c1 = min(c0 + per, A.num_scenes);
+    uint32_t mine = 0;
+#pragma unroll 8
+    for (uint32_t sc = c0; sc < c1; ++sc) mine += __ldcg(&out[sc].G2) * __ldcg(&out[sc].G3);
+    __shared__ uint32_t s_wsum[kFinishWarps];
+    uint32_t x = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) s_wsum[wid] = x;
+    __syncthreads();
+    uint32_t pre = 0, total = 0;
+#pragma unroll
+    for (int w = 0; w < kFinishWarps; ++w) {
+        const uint32_t v = s_wsum[w];
+        if ((uint32_t)w < wid) pre += v;
+        total += v;
+    }
+    uint32_t run = pre + x - mine;
+    for (uint32_t sc = c0; sc < c1; ++sc) {
+        out[sc].bucket_base = run;
+        run += __ldcg(&out[sc].G2) * __ldcg(&out[sc].G3);
+    }
     const uint32_t q = key_q_bits(A.key_bits, total);
-    if (lane == 0) {
+    if (tid == 0) {
         if (q == 0) atomicOr(&C->error, kErrCellRange);
         C->scenes_done = 0;
         if (temporal) {
@@ -471,9 +491,9 @@ __global__ void __launch_bounds__(32 * kFinishWarps) k_pca_finish_batch(BpScratc
         }
     }
     if (!temporal)
-        for (uint32_t k = lane; k < (uint32_t)kMaxPasses * 256u; k += 32) (&C->hist[0][0])[k] = 0u;
+        for (uint32_t k = tid; k < (uint32_t)kMaxPasses * 256u; k += kT) (&C->hist[0][0])[k] = 0u;
     const float qf = (float)(1u << q);
-    for (uint32_t s = lane; s < A.num_scenes; s += 32) out[s].q_scale = __fdiv_rn(qf, __ldcg(&out[s].q_range));
+    for (uint32_t sc = tid; sc < A.num_scenes; sc += kT) out[sc].q_scale = __fdiv_rn(qf, __ldcg(&out[sc].q_range));
 }
 
 cudaError_t launch_plan(const BpScratch& s, const BpArgs& a, cudaStream_t st) {

@@ -2,12 +2,11 @@
 // runs it in its last CTA per scene, and the library exports a host copy
 // (gsap_debug_scene_solve) so the solver can be checked without a GPU.
 //
-// FP64 where the result needs it: the covariance combine and the 3x3
-// symmetric eigensolve.  The solve runs a cyclic Jacobi in FP32 first (FP32
-// rotations are cheap on the GPU, FP64 ones are not) and then refines in
-// FP64 with a short chain of multiply-adds (eig3 below).  The grid choice
-// that follows is a heuristic (any grid gives the same pair set) and runs
-// in FP32.
+// FP64 where the result needs it: the covariance combine (sums about a
+// pilot point, so that the mean's square does not cancel the variance).  The
+// 3x3 symmetric eigensolve runs in FP32 (eig3 below), and so does the grid
+// choice that follows, a heuristic: any axes and any grid give the same pair
+// set.
 #pragma once
 #include "internal.cuh"
 #include <math.h>
@@ -65,50 +64,17 @@ __host__ __device__ inline void jacobi_sweeps(T a[3][3], T v[3][3], T tol, int m
     }
 }
 
-// V <- V (3I - V^T V) / 2: one Newton-Schulz step towards the orthogonal
-// polar factor of V (quadratic: an orthogonality error e becomes ~1.5 e^2).
-// Multiplies and adds only -- no divide or square root.
-__host__ __device__ inline void newton_schulz(double V[3][3]) {
-    double g[3][3], r[3][3];
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) g[i][j] = V[0][i] * V[0][j] + V[1][i] * V[1][j] + V[2][i] * V[2][j];
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) g[i][j] = ((i == j) ? 1.5 : 0.0) - 0.5 * g[i][j];
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) r[i][j] = V[i][0] * g[0][j] + V[i][1] * g[1][j] + V[i][2] * g[2][j];
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) V[i][j] = r[i][j];
-}
-
-// b = V^T a V (FP64).
-__host__ __device__ inline void rotate_into(const double a[3][3], const double V[3][3], double b[3][3]) {
-    double t[3][3];
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) t[i][j] = a[i][0] * V[0][j] + a[i][1] * V[1][j] + a[i][2] * V[2][j];
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) b[i][j] = V[0][i] * t[0][j] + V[1][i] * t[1][j] + V[2][i] * t[2][j];
-    for (int i = 0; i < 3; ++i)
-        for (int j = i + 1; j < 3; ++j) b[j][i] = b[i][j] = 0.5 * (b[i][j] + b[j][i]);
-}
-
-// Symmetric 3x3 eigensolve, FP64 result.  a is overwritten with the
-// diagonalised matrix, v receives the eigenvectors as columns.  Returns 0
-// when the first-order refinement sufficed, 1 when the FP64 rotations ran.
-//
-// Dependent FP64 operations are slow on this GPU (hundreds of cycles each),
-// so the FP64 part is kept to a short chain of multiply-adds:
-//   1. cyclic Jacobi in FP32 -> V32 (orthonormal to ~1e-7);
-//   2. V = V32 in FP64, one Newton-Schulz step (orthonormal to ~1e-14);
-//   3. B = V^T A V; its off-diagonal entries are ~1e-7 of the diagonal;
-//   4. when every pair is well separated (|b_pq| <= 1e-5 |b_qq - b_pp|),
-//      the first-order eigenvector correction V (I + E), E_pq = b_pq /
-//      (b_qq - b_pp) = -E_qp, leaves an error of order E^2 <= 1e-10; a
-//      second Newton-Schulz step restores orthonormality and the
-//      eigenvalues take their second-order terms, b_pp - sum_q b_pq E_pq;
-//   5. otherwise (near-degenerate spread) B is diagonalised by FP64 Jacobi
-//      rotations until its off-diagonal part reaches rounding level, as
-//      robust as a full FP64 Jacobi.
-__host__ __device__ inline int eig3(double a[3][3], double v[3][3]) {
+// Symmetric 3x3 eigensolve: cyclic Jacobi in FP32 on the covariance rounded
+// to FP32, to rounding level (a is overwritten with the diagonalised matrix,
+// v receives the eigenvectors as columns).  Eigenvalues come out within a few
+// FP32 ulps of the largest one and the axes orthonormal to ~1e-7, far more
+// than the sweep needs: any axes give the same pair set (the reference
+// itself sweeps along the largest-variance coordinate axis,
+// SapKernel.cu:63-97).  An FP64 refinement of these axes (Newton-Schulz
+// orthonormalisation and a first-order eigenvector correction) was measured
+// at 12 us more per 1M call for the one-scene finish: dependent FP64
+// operations take hundreds of cycles on this GPU.
+__host__ __device__ inline void eig3(double a[3][3], double v[3][3]) {
     float af[3][3], vf[3][3];
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) {
@@ -116,49 +82,11 @@ __host__ __device__ inline int eig3(double a[3][3], double v[3][3]) {
             vf[i][j] = (i == j) ? 1.f : 0.f;
         }
     jacobi_sweeps<float>(af, vf, 2.4e-7f, 12);
-    double V[3][3], b[3][3];
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) V[i][j] = vf[i][j];
-    newton_schulz(V);
-    rotate_into(a, V, b);
-    const int P[3] = {0, 0, 1}, Qi[3] = {1, 2, 2};
-    bool separated = true;
-    double E[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-    for (int k = 0; k < 3; ++k) {
-        const int p = P[k], q = Qi[k];
-        const double bpq = b[p][q], gap = b[q][q] - b[p][p];
-        if (bpq == 0.0) continue;
-        if (!(fabs(bpq) <= 1e-5 * fabs(gap))) { separated = false; break; }
-        E[p][q] = bpq / gap;
-        E[q][p] = -E[p][q];
-    }
-    if (separated) {
-        double W[3][3];
-        for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j) W[i][j] = V[i][j] + V[i][0] * E[0][j] + V[i][1] * E[1][j] + V[i][2] * E[2][j];
-        newton_schulz(W);
-        // second-order eigenvalues: lambda_p = b_pp - sum_q b_pq E_pq
-        for (int i = 0; i < 3; ++i) {
-            const double lam = b[i][i] - (b[i][0] * E[i][0] + b[i][1] * E[i][1] + b[i][2] * E[i][2]);
-            for (int j = 0; j < 3; ++j) {
-                v[i][j] = W[i][j];
-                a[i][j] = (i == j) ? lam : 0.0;
-            }
-        }
-        return 0;
-    }
-    newton_schulz(V);  // orthonormal to rounding level before the rotations
-    rotate_into(a, V, b);
-    double w[3][3];
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) w[i][j] = (i == j) ? 1.0 : 0.0;
-    jacobi_sweeps<double>(b, w, 4.4e-16, 16);
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) {
-            v[i][j] = V[i][0] * w[0][j] + V[i][1] * w[1][j] + V[i][2] * w[2][j];
-            a[i][j] = b[i][j];
+            a[i][j] = (i == j) ? (double)af[i][i] : 0.0;
+            v[i][j] = vf[i][j];
         }
-    return 1;
 }
 
 // Sums (FP64) of one scene -> axes, statistics and sweep grid.

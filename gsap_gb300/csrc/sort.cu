@@ -45,8 +45,10 @@ __device__ __forceinline__ uint32_t cta_excl_scan256(uint32_t v, uint32_t* s_w) 
     return pre + x - v;
 }
 
+// 4096-key tiles run two CTAs per SM (128 registers), 2048-key tiles four
+// (64 registers, no spills): the same keys in flight per SM either way.
 template <int ITEMS>
-__global__ void __launch_bounds__(kThreads, 2) k_onesweep(BpScratch S, const uint32_t* __restrict__ kin,
+__global__ void __launch_bounds__(kThreads, ITEMS <= 8 ? 4 : 2) k_onesweep(BpScratch S, const uint32_t* __restrict__ kin,
                                                        const uint32_t* __restrict__ vin,
                                                        uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
                                                        const uint32_t* count_ptr, uint32_t cap, int pass,
@@ -231,21 +233,28 @@ cudaError_t launch_sort_prep(const BpScratch& s, const uint32_t* keys, const uin
 
 cudaError_t launch_sort_pass(const BpScratch& s, int pass, int passes, const uint32_t* kin, const uint32_t* vin,
                              uint32_t* kout, uint32_t* vout, const uint32_t* count_ptr, uint64_t cap,
-                             uint32_t spin, cudaStream_t st, const SortGather* gather, bool count_next, int fmode) {
+                             uint32_t spin, cudaStream_t st, const SortGather* gather, bool count_next, int fmode,
+                             int tile) {
     SortGather G;
     if (gather) G = *gather;
     else G = SortGather{nullptr, nullptr, nullptr, nullptr};
-    static std::once_flag once[kMaxDevices];
-    static int val[kMaxDevices];
-    const int grid = per_device(once, val, [] {
+    static std::once_flag once[2][kMaxDevices];
+    static int val[2][kMaxDevices];
+    const int small = tile == kSortTileMin ? 1 : 0;
+    const int grid = per_device(once[small], val[small], [small] {
         int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_onesweep<kSortItems>, kThreads, 0);
+        if (small) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_onesweep<kSortItemsSmall>, kThreads, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_onesweep<kSortItems>, kThreads, 0);
         return sm_count() * (per_sm > 0 ? per_sm : 1);
     });
     uint32_t c = cap > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)cap;
     const int next = (count_next && pass + 1 < passes) ? 1 : 0;
-    k_onesweep<kSortItems><<<grid, kThreads, 0, st>>>(s, kin, vin, kout, vout, count_ptr, c, pass, spin, G, next,
-                                                      fmode);
+    if (small)
+        k_onesweep<kSortItemsSmall><<<grid, kThreads, 0, st>>>(s, kin, vin, kout, vout, count_ptr, c, pass, spin, G,
+                                                               next, fmode);
+    else
+        k_onesweep<kSortItems><<<grid, kThreads, 0, st>>>(s, kin, vin, kout, vout, count_ptr, c, pass, spin, G, next,
+                                                          fmode);
     return cudaGetLastError();
 }
 

@@ -82,7 +82,7 @@ class Sap:
 
     def __init__(self, max_n: int, mode: int = MODE_AABB, axis_mode: int = AXIS_PCA, max_scenes: int = 1,
                  entry_factor: int = 8, pair_factor: int = 16, sort_bits: int = 32, cell_factor: float = 2.0,
-                 spin_limit: int = 0, sort_mode: int = 0):
+                 spin_limit: int = 0, sort_mode: int = 0, sort_tile: int = 0):
         L = load()
         cfg = Config()
         L.gsap_config_default(C.byref(cfg))
@@ -90,6 +90,7 @@ class Sap:
         cfg.entry_factor, cfg.pair_factor, cfg.sort_bits = entry_factor, pair_factor, sort_bits
         cfg.cell_factor = cell_factor
         cfg.sort_mode = sort_mode
+        cfg.sort_tile = sort_tile
         if spin_limit:
             cfg.spin_limit = spin_limit
         self.cfg = cfg
@@ -163,7 +164,7 @@ class Sap:
     def autotune(self, mn: torch.Tensor, mx: torch.Tensor | None = None, offsets: torch.Tensor | None = None,
                  pairs: torch.Tensor | None = None, sorted: bool = True, graph: bool = True, reps: int = 3,
                  stream=None) -> dict:
-        """Picks the sort (bucket or radix), key width and cell factor for
+        """Picks the sort (bucket, or radix with its tile size), key width and cell factor for
         this kind of input by timing a small grid on it (gsap_sap_autotune);
         the handle keeps the fastest.  Returns the chosen settings."""
         n = mn.shape[0]
@@ -181,7 +182,7 @@ class Sap:
                                        C.c_uint32(flags), C.c_int(reps), C.byref(cfg),
                                        C.c_void_p(_stream_ptr(stream))))
         return {"sort_bits": int(cfg.sort_bits), "cell_factor": float(cfg.cell_factor),
-                "sort": "radix" if cfg.sort_mode == 0 else "bucket"}
+                "sort": "radix" if cfg.sort_mode == 0 else "bucket", "sort_tile": int(cfg.sort_tile)}
 
     def broadphase_async(self, mn, mx, pairs, d_count, sorted=False, graph=False, temporal=False, stream=None):
         """Asynchronous form: the pair count goes to the device tensor

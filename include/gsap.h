@@ -83,6 +83,7 @@ typedef struct gsap_config {
     float cell_factor;      /* cell size / mean projected width on the secondary axes (0 -> 2.0) */
     uint32_t spin_limit;    /* iteration cap of every device-side wait (0 -> default) */
     uint32_t sort_mode;     /* GSAP_SORT_* : how the sweep entries are sorted (0 -> radix) */
+    uint32_t sort_tile;     /* keys per radix tile of the broadphase sort: 2048 or 4096 (0 -> 4096) */
 } gsap_config;
 
 /* Sort of the sweep entries (the pair set is the same either way). */

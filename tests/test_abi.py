@@ -71,17 +71,20 @@ def solve(gsap_lib, pts, h, axis_mode=0, cell_factor=1.5, key_bits=32, entry_fac
 
 
 @pytest.mark.parametrize("seed", range(5))
-def test_fp64_eigensolve_matches_numpy(gsap_lib, seed):
+def test_eigensolve_matches_numpy(gsap_lib, seed):
+    """The scene solve (covariance in FP64, FP32 Jacobi) against numpy's
+    FP64 eigh: eigenvalues within a few FP32 ulps of the largest, axes
+    orthonormal and aligned to ~1e-7."""
     rng = np.random.default_rng(seed)
     R = np.linalg.qr(rng.normal(size=(3, 3)))[0]
     pts = (rng.normal(size=(5000, 3)) * [40.0, 9.0, 2.0]) @ R.T + rng.normal(size=3) * 100
     U, eig, mean, G2, G3 = solve(gsap_lib, pts, np.full((5000, 3), 0.3))
     C_ = np.cov(pts.T, bias=True)
     w, V = np.linalg.eigh(C_)
-    assert np.allclose(eig, w[::-1], rtol=1e-9, atol=1e-9)
-    for k in range(3):
-        assert abs(abs(U[k] @ V[:, 2 - k]) - 1.0) < 1e-9
-    assert np.allclose(U @ U.T, np.eye(3), atol=1e-12)
+    assert np.allclose(eig, w[::-1], rtol=0, atol=4e-7 * w.max())
+    for k in range(3):  # angle to numpy's axis below ~1.4e-5
+        assert 1.0 - abs(U[k] @ V[:, 2 - k]) / np.linalg.norm(U[k]) < 1e-10
+    assert np.allclose(U @ U.T, np.eye(3), atol=1e-6)
     assert np.linalg.det(U) > 0
     assert np.allclose(mean, pts.mean(0), rtol=1e-12, atol=1e-9)
     assert G2 >= 1 and G3 >= 1

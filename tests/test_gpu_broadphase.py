@@ -294,19 +294,19 @@ def test_autotune_keeps_the_pair_set(cuda, oracle_lib):
         assert np.array_equal(sub, oracle_lib.bf_aabb(mnb[a:b], mxb[a:b])), s
 
 
-@pytest.mark.parametrize("sort_mode", [0, 1])
+@pytest.mark.parametrize("sort_mode,sort_tile", [(0, 4096), (0, 2048), (1, 4096)])
 @pytest.mark.parametrize("sort_bits", [24, 32])
 @pytest.mark.parametrize("cell_factor", [0.5, 1.0, 2.0, 4.0])
-def test_every_setting_gives_the_same_pairs(cuda, oracle_lib, sort_bits, cell_factor, sort_mode):
-    """Sort (bucket or radix), key width and cell size only move work
-    between stages: the pair set is the brute force's for every setting the
-    autotuner may pick."""
+def test_every_setting_gives_the_same_pairs(cuda, oracle_lib, sort_bits, cell_factor, sort_mode, sort_tile):
+    """Sort (bucket, or radix with 4096- or 2048-key tiles), key width and
+    cell size only move work between stages: the pair set is the brute
+    force's for every setting the autotuner may pick."""
     from gsap_gb300 import Sap, scenes
     n = 30_000
     c, h, _ = scenes.aabb_gauss_parts(n, seed=21, std=(25.0, 6.0, 2.0))
     mn = np.concatenate([c - h, np.zeros((n, 1), np.float32)], 1)
     mx = np.concatenate([c + h, np.zeros((n, 1), np.float32)], 1)
-    sap = Sap(n, sort_bits=sort_bits, cell_factor=cell_factor, sort_mode=sort_mode)
+    sap = Sap(n, sort_bits=sort_bits, cell_factor=cell_factor, sort_mode=sort_mode, sort_tile=sort_tile)
     assert np.array_equal(run_bp(sap, mn, mx, cuda), oracle_lib.bf_aabb(mn, mx))
     assert np.array_equal(run_bp(sap, mn, mx, cuda, sorted=False), oracle_lib.bf_aabb(mn, mx))
 
@@ -519,3 +519,34 @@ def test_degenerate_and_far_from_origin_scenes(cuda, oracle_lib):
     mn = np.concatenate([far - h, np.zeros((4000, 1), np.float32)], 1)
     mx = np.concatenate([far + h, np.zeros((4000, 1), np.float32)], 1)
     assert np.array_equal(run_bp(sap, mn, mx, cuda), oracle_lib.bf_aabb(mn, mx))
+
+
+@pytest.mark.parametrize("both", [False, True])
+def test_sparse_pairs_reset_row_counters_between_calls(cuda, oracle_lib, both):
+    """Few pairs against many objects (fewer than n / 4): the scatter, not
+    the row scan, puts the touched rows' counters back to zero.  Calls on
+    one handle with different inputs, dense and sparse in turn, each equal
+    the brute force (a stale counter would shift the next call's rows)."""
+    from gsap_gb300 import MODE_SPHERE, Sap, scenes
+    n = 60_000
+    sap = Sap(n, mode=MODE_SPHERE if both else 0)
+    rng = np.random.default_rng(11)
+    for k, spread in enumerate((400.0, 40.0, 400.0, 900.0)):
+        c = rng.uniform(-spread, spread, (n, 3)).astype(np.float32)
+        if both:
+            import torch
+            sph = np.concatenate([c, np.full((n, 1), 0.5, np.float32)], 1)
+            pairs = torch.empty((16 * n, 2), dtype=torch.int32, device=cuda)
+            ent = torch.empty(n + 1, dtype=torch.int32, device=cuda)
+            n_pairs, n_ent = sap.collision(0.0, to_dev(sph, cuda), pairs, ent)
+            want_pairs, want_ent = oracle_lib.both_directions(oracle_lib.bf_sphere(sph))
+            assert np.array_equal(pairs[:n_pairs].cpu().numpy(), want_pairs), k
+            assert np.array_equal(ent[:n_ent].cpu().numpy(), want_ent), k
+        else:
+            h = np.full((n, 3), 0.5, np.float32)
+            mn = np.concatenate([c - h, np.zeros((n, 1), np.float32)], 1)
+            mx = np.concatenate([c + h, np.zeros((n, 1), np.float32)], 1)
+            want = oracle_lib.bf_aabb(mn, mx)
+            if spread > 100:
+                assert 4 * len(want) < n  # the sparse case
+            assert np.array_equal(run_bp(sap, mn, mx, cuda), want), k
