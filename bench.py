@@ -485,6 +485,9 @@ def _extra_small(args, dev, stream, out):
     ssap = Sap(16384)
     spairs = torch.empty((16 * 16384, 2), dtype=torch.int32, device=dev)
     scnt = torch.zeros(1, dtype=torch.int64, device=dev)
+    # autotuner (set-up, untimed), as for the 1M workload
+    stuned = None if args.no_tune else ssap.autotune(dsmn, dsmx, pairs=spairs, sorted=True, graph=True, reps=20,
+                                                     stream=stream)
     for _ in range(5):
         ssap.broadphase_async(dsmn, dsmx, spairs, scnt, sorted=True, graph=True, stream=stream)
     torch.cuda.synchronize()
@@ -496,7 +499,8 @@ def _extra_small(args, dev, stream, out):
     e1.record(stream)
     torch.cuda.synchronize()
     ssap.check()
-    small = {"n": 16384, "pairs": int(scnt.item()), "ms_per_call": round(e0.elapsed_time(e1) / 200, 4)}
+    small = {"n": 16384, "pairs": int(scnt.item()), "ms_per_call": round(e0.elapsed_time(e1) / 200, 4),
+             "settings": dict(stuned, autotuned=True) if stuned else {"autotuned": False}}
     if not args.no_cpu:
         import oracle
         oracle.build()
@@ -536,6 +540,9 @@ def _extra_demo(args, dev, stream, out):
     csap = Sap(nsp, mode=1)
     cpairs = torch.empty((40 * nsp, 2), dtype=torch.int32, device=dev)
     cent = torch.empty(nsp + 1, dtype=torch.int32, device=dev)
+    # autotuner (set-up, untimed) on the same spheres; the collision calls use its settings
+    ctuned = None if args.no_tune else csap.autotune(dsph, None, pairs=cpairs, sorted=True, graph=True, reps=20,
+                                                     stream=stream)
     for _ in range(5):
         npc, nec = csap.collision(0.0, dsph, cpairs, cent, stream=stream)
     h0 = time.perf_counter()
@@ -547,7 +554,8 @@ def _extra_demo(args, dev, stream, out):
     coll = {"spheres": nsp, "pairs_both_directions": npc, "pair_entries": nec,
             "ms_per_call": round((time.perf_counter() - h0) * 10, 4),
             "device_ms_per_call": round(e0.elapsed_time(e1) / 100, 4),
-            "note": "gsap_sap_collision blocks for the host counts each call, as Sap::collision does"}
+            "note": "gsap_sap_collision blocks for the host counts each call, as Sap::collision does",
+            "settings": dict(ctuned, autotuned=True) if ctuned else {"autotuned": False}}
     if not args.no_cpu:
         import oracle
         sp = dsph.cpu().numpy()

@@ -9,6 +9,7 @@
 // fixed sequence of launches on the caller's stream (optionally a cached
 // CUDA graph) followed, only when the caller asks for host counts, by one
 // small read of the control block.
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -196,7 +197,8 @@ extern "C" gsap_sap* gsap_sap_create(uint32_t max_n, const gsap_config* cfg) {
     A((void**)&s.ctrl, sizeof(Ctrl));
     A((void**)&s.scenes, sizeof(Scene) * c.max_scenes);
     A((void**)&s.scenes_next, sizeof(Scene) * c.max_scenes);
-    A((void**)&s.partials, sizeof(PcaPartial) * s.max_work);
+    // one partial per PCA CTA: per work item, or kPcaSplitSmall per item for small calls
+    A((void**)&s.partials, sizeof(PcaPartial) * std::max<uint64_t>(s.max_work, (uint64_t)kPcaSmallWork * kPcaSplitSmall));
     A((void**)&s.scene_done, 4ull * c.max_scenes);
     A((void**)&s.work_start, 4ull * (c.max_scenes + 1));
     if (c.max_scenes > 1) A((void**)&s.objscene, 4ull * max_n);

@@ -21,6 +21,10 @@ int per_device(std::once_flag (&once)[kMaxDevices], int (&val)[kMaxDevices], F c
 }
 
 constexpr int kChunk = 4096;          // objects per PCA / projection work item
+// Calls of at most kPcaSmallWork work items run kPcaSplitSmall PCA CTAs per
+// item (one object per thread), each with its own partial.
+constexpr uint32_t kPcaSmallWork = 64;
+constexpr uint32_t kPcaSplitSmall = 16;
 constexpr int kThreads = 256;         // threads per CTA of the streaming kernels
 constexpr int kMaxPasses = 4;         // radix passes (8-bit digits, <= 32-bit keys)
 constexpr int kSortItems = 16;        // keys per thread in a onesweep tile (default)

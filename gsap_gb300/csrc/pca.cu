@@ -80,12 +80,21 @@ __device__ __forceinline__ void pilot_of(const BpArgs& A, uint32_t sb, uint32_t 
 
 // ---------------------------------------------------------------- K1
 
-__global__ void __launch_bounds__(kThreads) k_pca(BpScratch S, BpArgs A) {
+// split CTAs per work item, each over kChunk / split of its objects, each
+// writing its own partial (partial index = CTA index): calls of a few work
+// items spread over more SMs (kPcaSplitSmall), large calls take one CTA per
+// item.
+__global__ void __launch_bounds__(kThreads) k_pca(BpScratch S, BpArgs A, uint32_t split) {
     __shared__ float s_red[kThreads / 32][2 * kPcaQ + 3];
     const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     uint32_t scene, b, e, wfirst, nw;
-    if (!map_work(blockIdx.x, S, A, scene, b, e, wfirst, nw)) return;
+    if (!map_work(blockIdx.x / split, S, A, scene, b, e, wfirst, nw)) return;
     const uint32_t sb = scene_begin(A, scene), se = scene_end(A, scene);
+    {
+        const uint32_t part = kChunk / split, sub = blockIdx.x % split;
+        b = min(e, b + sub * part);
+        e = min(e, b + part);
+    }
 
     // pilot = centre of the scene's first object (shift against cancellation)
     float px = 0.f, py = 0.f, pz = 0.f;
@@ -198,7 +207,8 @@ __device__ __forceinline__ void reset_counters(Ctrl* C) {
     C->iters = 0ull;
 }
 
-__global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, uint64_t entry_cap, int temporal) {
+__global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, uint64_t entry_cap, int temporal,
+                                                         uint32_t split) {
     Scene* const out = temporal ? S.scenes_next : S.scenes;
     __shared__ uint32_t s_flag;
     const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -209,7 +219,7 @@ __global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, 
     // (bad offsets can plan more work items than were launched: only
     // partials that k_pca wrote are read)
     const uint32_t nw0 = A.scene_off ? S.work_start[scene + 1] - wfirst : work_items(A.n);
-    const uint32_t nw = wfirst < A.num_work ? min(nw0, A.num_work - wfirst) : 0u;
+    const uint32_t nw = (wfirst < A.num_work ? min(nw0, A.num_work - wfirst) : 0u) * split;
     // Thread 0's loads for later (the pilot object, and the epoch that the
     // one-scene reset below advances) are in flight during the merge.
     const bool one = A.num_scenes == 1;
@@ -227,7 +237,7 @@ __global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, 
 #pragma unroll
     for (int q = 0; q < kPcaQ; ++q) { ah[q] = 0.f; al[q] = 0.f; }
     for (uint32_t k = tid; k < nw; k += kThreads) {
-        const PcaPartial* P = &S.partials[wfirst + k];
+        const PcaPartial* P = &S.partials[wfirst * split + k];
 #pragma unroll
         for (int q = 0; q < kPcaQ; ++q) kahan_merge(ah[q], al[q], P->hi[q], P->lo[q]);
 #pragma unroll
@@ -376,7 +386,7 @@ __global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, 
 constexpr int kFinishWarps = 16;
 constexpr int kFinishScenes = 32;
 __global__ void __launch_bounds__(32 * kFinishWarps) k_pca_finish_batch(BpScratch S, BpArgs A, uint64_t entry_cap,
-                                                                       int temporal) {
+                                                                       int temporal, uint32_t split) {
     __shared__ SceneSums s_z[kFinishScenes];
     Scene* const out = temporal ? S.scenes_next : S.scenes;
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -388,14 +398,14 @@ __global__ void __launch_bounds__(32 * kFinishWarps) k_pca_finish_batch(BpScratc
         const uint32_t sb = scene_begin(A, scene), se = scene_end(A, scene);
         const uint32_t wfirst = S.work_start[scene];
         const uint32_t nw0 = S.work_start[scene + 1] - wfirst;
-        const uint32_t nw = wfirst < A.num_work ? min(nw0, A.num_work - wfirst) : 0u;
+        const uint32_t nw = (wfirst < A.num_work ? min(nw0, A.num_work - wfirst) : 0u) * split;
         float px = 0.f, py = 0.f, pz = 0.f;
         if (lane == 0) pilot_of(A, sb, se, px, py, pz);
         float ah[kPcaQ], al[kPcaQ], am[3] = {0.f, 0.f, 0.f};
 #pragma unroll
         for (int q = 0; q < kPcaQ; ++q) { ah[q] = 0.f; al[q] = 0.f; }
         for (uint32_t j = lane; j < nw; j += 32) {
-            const PcaPartial* P = &S.partials[wfirst + j];
+            const PcaPartial* P = &S.partials[wfirst * split + j];
 #pragma unroll
             for (int q = 0; q < kPcaQ; ++q) kahan_merge(ah[q], al[q], P->hi[q], P->lo[q]);
 #pragma unroll
@@ -502,12 +512,13 @@ cudaError_t launch_plan(const BpScratch& s, const BpArgs& a, cudaStream_t st) {
 }
 
 cudaError_t launch_pca(const BpScratch& s, const BpArgs& a, cudaStream_t st, int temporal) {
-    k_pca<<<a.num_work, kThreads, 0, st>>>(s, a);
+    const uint32_t split = a.num_work <= kPcaSmallWork ? kPcaSplitSmall : 1u;
+    k_pca<<<a.num_work * split, kThreads, 0, st>>>(s, a, split);
     if (a.num_scenes > 1)
         k_pca_finish_batch<<<(a.num_scenes + kFinishScenes - 1) / kFinishScenes, 32 * kFinishWarps, 0, st>>>(
-            s, a, s.entry_cap, temporal);
+            s, a, s.entry_cap, temporal, split);
     else
-        k_pca_finish<<<1, kThreads, 0, st>>>(s, a, s.entry_cap, temporal);
+        k_pca_finish<<<1, kThreads, 0, st>>>(s, a, s.entry_cap, temporal, split);
     return cudaGetLastError();
 }
 

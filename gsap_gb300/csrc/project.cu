@@ -38,15 +38,23 @@ __device__ __forceinline__ bool load_box(const BpArgs& A, uint32_t i, float3& a,
     return isfinite(a.x) && isfinite(a.y) && isfinite(a.z) && isfinite(b.x) && isfinite(b.y) && isfinite(b.z);
 }
 
-constexpr int kProjItems = 8;                          // objects per thread
-constexpr int kProjHalf = kThreads * kProjItems;       // objects per CTA: half a work chunk
-constexpr int kProjSplit = kChunk / kProjHalf;         // CTAs per work chunk
+// ITEMS objects per thread, kThreads * ITEMS per CTA, kChunk / that CTAs
+// per work item.  Large calls take 8 per thread (fewer CTAs, so fewer
+// histogram atomics on the 256 shared counters); small calls (a few work
+// items) take 1, so that the objects spread over 16 CTAs per work item
+// instead of 2 and no thread walks 8 objects in turn.
+constexpr int kProjItemsLarge = 8;
+constexpr int kProjItemsSmall = 1;
+constexpr uint32_t kProjSmallWork = 64;  // work items (64 x 4096 objects) up to which calls count as small
 
 // PASSES > 0: counts the first radix digit for the onesweep passes;
 // PASSES == 0 (bucket sort): counts the entries of every sub-bucket instead
 // (global atomics; sub_layout in internal.cuh).
-template <int PASSES>
+template <int PASSES, int ITEMS>
 __global__ void __launch_bounds__(kThreads) k_project(BpScratch S, BpArgs A) {
+    constexpr int kProjItems = ITEMS;
+    constexpr int kProjHalf = kThreads * kProjItems;  // objects per CTA
+    constexpr int kProjSplit = kChunk / kProjHalf;    // CTAs per work item
     __shared__ uint32_t s_hist[PASSES > 0 ? PASSES : 1][256];
     __shared__ float s_f[16];
     __shared__ uint32_t s_i[4];
@@ -158,9 +166,17 @@ __global__ void __launch_bounds__(kThreads) k_project(BpScratch S, BpArgs A) {
 }
 
 cudaError_t launch_project(const BpScratch& s, const BpArgs& a, int passes, cudaStream_t st) {
-    if (passes == 0) k_project<0><<<a.num_work * kProjSplit, kThreads, 0, st>>>(s, a);
-    else if (passes == 3) k_project<3><<<a.num_work * kProjSplit, kThreads, 0, st>>>(s, a);
-    else k_project<4><<<a.num_work * kProjSplit, kThreads, 0, st>>>(s, a);
+    if (a.num_work <= kProjSmallWork) {
+        constexpr int kSplit = kChunk / (kThreads * kProjItemsSmall);
+        if (passes == 0) k_project<0, kProjItemsSmall><<<a.num_work * kSplit, kThreads, 0, st>>>(s, a);
+        else if (passes == 3) k_project<3, kProjItemsSmall><<<a.num_work * kSplit, kThreads, 0, st>>>(s, a);
+        else k_project<4, kProjItemsSmall><<<a.num_work * kSplit, kThreads, 0, st>>>(s, a);
+    } else {
+        constexpr int kSplit = kChunk / (kThreads * kProjItemsLarge);
+        if (passes == 0) k_project<0, kProjItemsLarge><<<a.num_work * kSplit, kThreads, 0, st>>>(s, a);
+        else if (passes == 3) k_project<3, kProjItemsLarge><<<a.num_work * kSplit, kThreads, 0, st>>>(s, a);
+        else k_project<4, kProjItemsLarge><<<a.num_work * kSplit, kThreads, 0, st>>>(s, a);
+    }
     return cudaGetLastError();
 }
 

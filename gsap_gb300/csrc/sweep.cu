@@ -115,13 +115,16 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
 
     // Work is taken kGrab chunks of 32 entries at a time: every atomic on the
     // one shared counter serialises at its L2 slice, so fewer, larger grabs.
+    // With fewer entries than kGrab chunks for every warp of the grid (small
+    // calls), one chunk at a time, so that the work spreads over all warps.
+    const uint32_t grab = (uint64_t)E >= (uint64_t)gridDim.x * kWarps * 32u * kGrab ? 32u * kGrab : 32u;
     uint32_t base = 0, grab_end = 0;
     while (true) {
         if (base >= grab_end) {
             uint32_t g = 0;
-            if (lane == 0) g = atomicAdd(&C->sweep_ctr, 32u * kGrab);
+            if (lane == 0) g = atomicAdd(&C->sweep_ctr, grab);
             base = __shfl_sync(0xffffffffu, g, 0);
-            grab_end = base + 32u * kGrab;
+            grab_end = base + grab;
         }
         if (base >= E) break;
         const uint32_t e = base + lane;
