@@ -708,8 +708,14 @@ def _extra_rigid(args, dev, stream, out):
     prb.load_scene(sc)
     prb.set_contact(model=CONTACT_CONFIG, **cfgp)
     init = {k: np.ascontiguousarray(sc[k], np.float32) for k in ("pos", "quat", "lin_vel", "ang_vel")}
-    rsap = Sap(nb, sort_bits=24)  # the key width the autotuner picks for the 1M scene
-    rb = {"bodies": nb, "particles": sc["n_particles"]}
+    rsap = Sap(nb, sort_bits=24)
+    # autotuner (set-up, untimed) on the body AABBs of the initial pose
+    rtuned = None
+    if not args.no_tune:
+        bmn, bmx = scenes.body_aabbs(sc)
+        rtuned = rsap.autotune(torch.from_numpy(bmn).to(dev), torch.from_numpy(bmx).to(dev), reps=20, stream=stream)
+    rb = {"bodies": nb, "particles": sc["n_particles"],
+          "broadphase_settings": dict(rtuned, autotuned=True) if rtuned else {"autotuned": False, "sort_bits": 24}}
     if not args.no_cpu:
         import oracle
         from oracle.trajectory import fp64_errors
@@ -808,7 +814,14 @@ def _extra_rigid_batched(args, dev, stream, out):
     bprb.set_scenes(bo)
     binit = {k: np.ascontiguousarray(ms_[k], np.float32) for k in ("pos", "quat", "lin_vel", "ang_vel")}
     bsap2 = Sap(nbb, max_scenes=args.rb_scenes)
-    rbb = {"scenes": args.rb_scenes, "bodies": nbb, "particles": ms_["n_particles"]}
+    # autotuner (set-up, untimed) on the body AABBs of the initial pose
+    rbtuned = None
+    if not args.no_tune:
+        bmn, bmx = scenes.body_aabbs(ms_)
+        rbtuned = bsap2.autotune(torch.from_numpy(bmn).to(dev), torch.from_numpy(bmx).to(dev),
+                                 offsets=torch.from_numpy(np.asarray(bo, np.int32)).to(dev), reps=5, stream=stream)
+    rbb = {"scenes": args.rb_scenes, "bodies": nbb, "particles": ms_["n_particles"],
+           "broadphase_settings": dict(rbtuned, autotuned=True) if rbtuned else {"autotuned": False}}
     if not args.no_cpu:
         from oracle.trajectory import fp64_errors
         t0 = time.perf_counter()

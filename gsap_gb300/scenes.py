@@ -186,6 +186,37 @@ def mixed_scenes(S: int = 1024, seed: int = 0, lo: int = 256, hi: int = 8192, bo
     return out
 
 
+def body_aabbs(sc: dict):
+    """Body AABBs of a rigid-body scene dict at its current pose (particle
+    centres x + R(q) ref, +/- radius), as (n, 4) float32 min / max arrays:
+    the broadphase input of the config-model step, for tuning a body
+    broadphase handle (Sap.autotune) before stepping."""
+    q = np.asarray(sc["quat"], np.float64)
+    q = q / np.linalg.norm(q, axis=1, keepdims=True)
+    x, y, z, w = q[:, 0], q[:, 1], q[:, 2], q[:, 3]
+    R = np.stack([np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)], 1),
+                  np.stack([2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)], 1),
+                  np.stack([2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)], 1)], 1)
+    pos = np.asarray(sc["pos"], np.float64)[:, :3]
+    ref = np.asarray(sc["ref_pos"], np.float64)
+    shape = np.asarray(sc["shape_idx"], np.int64)
+    npart = np.asarray(sc["n_part"], np.int64)
+    n = len(pos)
+    lo = np.full((n, 3), np.inf)
+    hi = np.full((n, 3), -np.inf)
+    for k in range(int(npart.max()) if n else 0):
+        m = npart > k
+        rk = ref[shape[m] * MAXP + k]
+        c = pos[m] + np.einsum("bij,bj->bi", R[m], rk[:, :3])
+        lo[m] = np.minimum(lo[m], c - rk[:, 3:4])
+        hi[m] = np.maximum(hi[m], c + rk[:, 3:4])
+    mn = np.zeros((n, 4), np.float32)
+    mx = np.zeros((n, 4), np.float32)
+    mn[:, :3] = lo
+    mx[:, :3] = hi
+    return mn, mx
+
+
 def subset_bodies(sc: dict, a: int, z: int) -> dict:
     """Bodies [a, z) of a scene dict as a scene of their own (particle
     starts re-based; shape tables shared)."""

@@ -41,3 +41,22 @@ def test_batched_case_sizes_and_offsets():
     h = 0.5 * (mx[:, :3] - mn[:, :3])
     assert h.min() >= 0.1 - 1e-5 and h.max() <= 0.5 + 1e-5
     assert np.all(mn[:, 3] == 0) and np.all(mx[:, 3] == 0)
+
+
+def test_body_aabbs_bound_every_particle(oracle_lib):
+    """scenes.body_aabbs (the tuning input of a body broadphase) equals the
+    union of the particle spheres that the FP64 oracle places at the same
+    pose (after one of its steps), to FP32 rounding."""
+    sc = scenes.mixed_scenes(S=3, seed=2, lo=64, hi=256)
+    st = scenes.to_f64(sc)
+    oracle_lib.rb_step_cfg_f64(st, dict(dt=1.0 / 600.0, k=2e4, eta=50.0, kt=0.1, gravity_y=-9.81,
+                                        box_lo=(0.0, 0.0, 0.0), box_hi=(100.0, 100.0, 100.0)))
+    moved = dict(sc, pos=st["pos"], quat=st["quat"])
+    mn, mx = scenes.body_aabbs(moved)
+    p = st["p_pos"]  # particle centres and radii at the stepped pose
+    owner = np.repeat(np.arange(len(sc["pos"])), sc["n_part"])
+    lo = np.full((len(sc["pos"]), 3), np.inf)
+    hi = np.full((len(sc["pos"]), 3), -np.inf)
+    np.minimum.at(lo, owner, p[:, :3] - p[:, 3:4])
+    np.maximum.at(hi, owner, p[:, :3] + p[:, 3:4])
+    assert np.allclose(mn[:, :3], lo, rtol=0, atol=1e-4) and np.allclose(mx[:, :3], hi, rtol=0, atol=1e-4)
