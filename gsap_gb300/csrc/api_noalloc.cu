@@ -17,8 +17,7 @@
 //
 // Set-up: the first call on each device looks the array up with
 // cudaGetSymbolAddress and zeroes its control block and look-back words
-// (synchronously).  Make that first call before any stream capture begins.
-// Later calls look the address up again (this allocates nothing); a failed
+// (synchronously).  Later calls look the address up again (this allocates nothing); a failed
 // set-up is not remembered, so the next call retries it, and an address
 // that changed (the module was loaded again after cudaDeviceReset) gets a
 // fresh set-up.

@@ -46,12 +46,13 @@ __device__ __forceinline__ bool load_box(const BpArgs& A, uint32_t i, float3& a,
 constexpr int kProjItemsLarge = 8;
 constexpr int kProjItemsSmall = 1;
 constexpr uint32_t kProjSmallWork = 64;  // work items (64 x 4096 objects) up to which calls count as small
+constexpr int kProjStage = 128;          // entries of one item staged per warp
 
 // PASSES > 0: counts the first radix digit for the onesweep passes;
 // PASSES == 0 (bucket sort): counts the entries of every sub-bucket instead
 // (global atomics; sub_layout in internal.cuh).
 template <int PASSES, int ITEMS>
-__global__ void __launch_bounds__(kThreads) k_project(BpScratch S, BpArgs A) {
+__global__ void __launch_bounds__(kThreads, 4) k_project(BpScratch S, BpArgs A) {
     constexpr int kProjItems = ITEMS;
     constexpr int kProjHalf = kThreads * kProjItems;  // objects per CTA
     constexpr int kProjSplit = kChunk / kProjHalf;    // CTAs per work item
@@ -60,6 +61,8 @@ __global__ void __launch_bounds__(kThreads) k_project(BpScratch S, BpArgs A) {
     __shared__ uint32_t s_i[4];
     __shared__ uint32_t s_wtot[kThreads / 32];
     __shared__ uint32_t s_base;
+    // per warp: the entries of one item, staged for coalesced stores
+    __shared__ uint32_t s_sk[kThreads / 32][kProjStage], s_sv[kThreads / 32][kProjStage];
     const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     uint32_t scene, b, e, wfirst, nw;
     if (!map_work(blockIdx.x / kProjSplit, S, A, scene, b, e, wfirst, nw)) return;
@@ -135,25 +138,55 @@ __global__ void __launch_bounds__(kThreads) k_project(BpScratch S, BpArgs A) {
     }
     __syncthreads();
     const uint64_t wpos = (uint64_t)s_base + s_wtot[wid];
+    // Entries of item k of this warp occupy [wpos + base_k, wpos + base_k +
+    // tot_k) (item-major, lanes in order).  When they fit the warp's stage
+    // they are written there first and then stored by all 32 lanes in
+    // order (coalesced, and the histogram counts run on full warps); an item
+    // with more entries (objects spanning many cells) is stored lane by lane.
 #pragma unroll
     for (int k = 0; k < kProjItems; ++k) {
-        uint32_t n2 = ncl[k] >> 16, n3 = ncl[k] & 0xFFFFu;
-        if (n2 * n3 == 0) continue;
-        uint32_t i = wb + k * 32 + lane;
-        uint32_t c2a = clo[k] >> 16, c3a = clo[k] & 0xFFFFu;
-        uint64_t pos = wpos + pre[k];
-        for (uint32_t x2 = 0; x2 < n2; ++x2)
-            for (uint32_t x3 = 0; x3 < n3; ++x3, ++pos) {
-                uint32_t key = ((bb + (c2a + x2) * G3 + (c3a + x3)) << Q) | qlo[k];
-                if (pos < S.entry_cap) {  // entries past the capacity are counted, never stored
+        const uint32_t n2 = ncl[k] >> 16, n3 = ncl[k] & 0xFFFFu;
+        const uint32_t i = wb + k * 32 + lane;
+        const uint32_t c2a = clo[k] >> 16, c3a = clo[k] & 0xFFFFu;
+        const uint32_t base_k = __shfl_sync(0xffffffffu, pre[k], 0);
+        const uint32_t end_k = (k + 1 < kProjItems) ? __shfl_sync(0xffffffffu, pre[k + 1 < kProjItems ? k + 1 : k], 0)
+                                                    : running;
+        const uint32_t tot_k = end_k - base_k;
+        if (tot_k <= (uint32_t)kProjStage) {
+            uint32_t o = pre[k] - base_k;
+            for (uint32_t x2 = 0; x2 < n2; ++x2)
+                for (uint32_t x3 = 0; x3 < n3; ++x3, ++o) {
                     // owner flags: is this the object's lowest cell on u2 / u3?
                     const uint32_t fl = (x2 == 0 ? 1u : 0u) | (x3 == 0 ? 2u : 0u);
+                    s_sk[wid][o] = ((bb + (c2a + x2) * G3 + (c3a + x3)) << Q) | qlo[k];
+                    s_sv[wid][o] = i | (fl << kFlagShift);
+                }
+            __syncwarp();
+            for (uint32_t j = lane; j < tot_k; j += 32) {
+                const uint64_t pos = wpos + base_k + j;
+                if (pos < S.entry_cap) {  // entries past the capacity are counted, never stored
+                    const uint32_t key = s_sk[wid][j];
                     S.keys[0][pos] = key;
-                    S.vals[0][pos] = i | (fl << kFlagShift);
+                    S.vals[0][pos] = s_sv[wid][j];
                     if (PASSES > 0) atomicAdd(&s_hist[0][key & 255u], 1u);  // later digits: counted by the sort passes
                     else atomicAdd(&S.subcnt[min(key >> sub_shift, kMaxSub - 1u)], 1u);
                 }
             }
+            __syncwarp();  // the stage is refilled by the next item
+        } else {
+            uint64_t pos = wpos + pre[k];
+            for (uint32_t x2 = 0; x2 < n2; ++x2)
+                for (uint32_t x3 = 0; x3 < n3; ++x3, ++pos) {
+                    const uint32_t key = ((bb + (c2a + x2) * G3 + (c3a + x3)) << Q) | qlo[k];
+                    if (pos < S.entry_cap) {
+                        const uint32_t fl = (x2 == 0 ? 1u : 0u) | (x3 == 0 ? 2u : 0u);
+                        S.keys[0][pos] = key;
+                        S.vals[0][pos] = i | (fl << kFlagShift);
+                        if (PASSES > 0) atomicAdd(&s_hist[0][key & 255u], 1u);
+                        else atomicAdd(&S.subcnt[min(key >> sub_shift, kMaxSub - 1u)], 1u);
+                    }
+                }
+        }
     }
     }
     if (bad) atomicOr(&S.ctrl->error, kErrNonFinite);

@@ -221,8 +221,7 @@ gsap_status gsap_radix_sort_f32(gsap_sap* h, float* d_keys, uint32_t* d_vals, ui
  *     GSAP_ERR_CAPACITY before any work is queued.
  *   - The first call on each device does the set-up (looks up the array,
  *     zeroes its control block and look-back words, synchronises the
- *     device); make it before any stream capture begins.  A set-up that
- *     failed is retried by the next call.
+ *     device).  A set-up that failed is retried by the next call.
  *   - d_keys / d_vals must be device memory of the current device; other
  *     pointers return GSAP_ERR_INVALID before any work is queued.
  *   - One scratch per device: calls that overlap in time (other streams,
