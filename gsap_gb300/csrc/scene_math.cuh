@@ -74,19 +74,10 @@ __host__ __device__ inline void jacobi_sweeps(T a[3][3], T v[3][3], T tol, int m
 // orthonormalisation and a first-order eigenvector correction) was measured
 // at 12 us more per 1M call for the one-scene finish: dependent FP64
 // operations take hundreds of cycles on this GPU.
-__host__ __device__ inline void eig3(double a[3][3], double v[3][3]) {
-    float af[3][3], vf[3][3];
+__host__ __device__ inline void eig3(float a[3][3], float v[3][3]) {
     for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) {
-            af[i][j] = (float)a[i][j];
-            vf[i][j] = (i == j) ? 1.f : 0.f;
-        }
-    jacobi_sweeps<float>(af, vf, 2.4e-7f, 12);
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) {
-            a[i][j] = (i == j) ? (double)af[i][i] : 0.0;
-            v[i][j] = vf[i][j];
-        }
+        for (int j = 0; j < 3; ++j) v[i][j] = (i == j) ? 1.f : 0.f;
+    jacobi_sweeps<float>(a, v, 2.4e-7f, 12);
 }
 
 // Sums (FP64) of one scene -> axes, statistics and sweep grid.
@@ -108,7 +99,9 @@ __host__ __device__ inline void choose_scene(const SceneSums& z, const BpArgs& A
         for (int j = 0; j < 3; ++j) C[i][j] = z.sdd[idx[i][j]] * inv_n - md[i] * md[j];
     double mean[3] = {z.pilot[0] + md[0], z.pilot[1] + md[1], z.pilot[2] + md[2]};
 
-    double U[3][3], lam[3];
+    // From here on FP32 (the FP64 fields of the record are written from it):
+    // serial FP64 operations are slow on this GPU, and the axes need no more.
+    float U[3][3], lam[3];
     if (A.axis_mode == 1) {
         // axisVecMultiple (SapKernel.cu:63-97): largest diagonal entry, the
         // reference's tie order, fixed secondary axes.
@@ -118,16 +111,16 @@ __host__ __device__ inline void choose_scene(const SceneSums& z, const BpArgs& A
         int a1 = ax == 0 ? 1 : 0, a2 = 3 - ax - a1;
         int order[3] = {ax, a1, a2};
         for (int r = 0; r < 3; ++r) {
-            for (int c = 0; c < 3; ++c) U[r][c] = (c == order[r]) ? 1.0 : 0.0;
-            lam[r] = C[order[r]][order[r]];
+            for (int c = 0; c < 3; ++c) U[r][c] = (c == order[r]) ? 1.f : 0.f;
+            lam[r] = (float)C[order[r]][order[r]];
         }
     } else {
-        double a[3][3], v[3][3];
+        float a[3][3], v[3][3];
         for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j) a[i][j] = 0.5 * (C[i][j] + C[j][i]);
+            for (int j = 0; j < 3; ++j) a[i][j] = (float)(0.5 * (C[i][j] + C[j][i]));
         eig3(a, v);
         int o[3] = {0, 1, 2};
-        double ev[3] = {a[0][0], a[1][1], a[2][2]};
+        float ev[3] = {a[0][0], a[1][1], a[2][2]};
         // descending eigenvalues, stable on ties
         for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 2 - i; ++j)
@@ -137,8 +130,8 @@ __host__ __device__ inline void choose_scene(const SceneSums& z, const BpArgs& A
             for (int c = 0; c < 3; ++c) U[r][c] = v[c][o[r]];
             // sign: largest-magnitude component positive (lowest index on ties)
             int m = 0;
-            for (int c = 1; c < 3; ++c) if (fabs(U[r][c]) > fabs(U[r][m])) m = c;
-            if (U[r][m] < 0) for (int c = 0; c < 3; ++c) U[r][c] = -U[r][c];
+            for (int c = 1; c < 3; ++c) if (fabsf(U[r][c]) > fabsf(U[r][m])) m = c;
+            if (U[r][m] < 0.f) for (int c = 0; c < 3; ++c) U[r][c] = -U[r][c];
         }
         // right-handed frame
         U[2][0] = U[0][1] * U[1][2] - U[0][2] * U[1][1];
@@ -150,7 +143,7 @@ __host__ __device__ inline void choose_scene(const SceneSums& z, const BpArgs& A
         out.mean[r] = mean[r];
         for (int c = 0; c < 3; ++c) {
             out.axes[3 * r + c] = U[r][c];
-            out.u[3 * r + c] = (float)U[r][c];
+            out.u[3 * r + c] = U[r][c];
         }
     }
     // ---- grid choice: a heuristic, FP32 from here on
