@@ -550,3 +550,24 @@ def test_sparse_pairs_reset_row_counters_between_calls(cuda, oracle_lib, both):
             if spread > 100:
                 assert 4 * len(want) < n  # the sparse case
             assert np.array_equal(run_bp(sap, mn, mx, cuda), want), k
+
+
+def test_objects_spanning_many_cells(cuda, oracle_lib):
+    """A few boxes hundreds of cells wide among small ones: the projection
+    writes such objects' entries lane by lane (more entries per warp item
+    than its shared-memory stage holds) and the rest through the stage; the
+    pair set is the brute force's."""
+    from gsap_gb300 import Sap
+    rng = np.random.default_rng(17)
+    n = 20_000
+    c = rng.normal(0.0, [60.0, 12.0, 4.0], (n, 3)).astype(np.float32)
+    h = rng.uniform(0.1, 0.6, (n, 3)).astype(np.float32)
+    big = rng.choice(n, 40, replace=False)
+    h[big] = rng.uniform(5.0, 15.0, (40, 3))  # each spans tens to hundreds of cells
+    mn = np.concatenate([c - h, np.zeros((n, 1), np.float32)], 1)
+    mx = np.concatenate([c + h, np.zeros((n, 1), np.float32)], 1)
+    want = oracle_lib.bf_aabb(mn, mx)
+    for cf in (0.5, 2.0):
+        sap = Sap(n, cell_factor=cf, entry_factor=64, pair_factor=64)
+        assert np.array_equal(run_bp(sap, mn, mx, cuda), want), cf
+        assert sap.stats()["entries"] > n + 1000  # the big boxes really replicate
