@@ -582,8 +582,9 @@ def _extra_large(args, dev, stream, out):
     (lmn, lmx), = make_inputs(0, nl, 1)[0]
     dlmn, dlmx = torch.from_numpy(lmn).to(dev), torch.from_numpy(lmx).to(dev)
     del lmn, lmx
-    lsap = Sap(nl)
-    lcfg = lsap.autotune(dlmn, dlmx, reps=3)
+    lsap = Sap(nl, sort_bits=args.sort_bits or 32, cell_factor=args.cell_factor or 2.0)
+    lcfg = (dict(sort_bits=args.sort_bits or 32, cell_factor=args.cell_factor or 2.0, autotuned=False)
+            if args.no_tune else lsap.autotune(dlmn, dlmx, reps=5))
     lpairs = torch.empty((8 * nl, 2), dtype=torch.int32, device=dev)
     lcnt = torch.zeros(1, dtype=torch.int64, device=dev)
     for _ in range(3):

@@ -124,6 +124,7 @@ struct BpScratch {
     uint32_t* scene_done;      // per-scene PCA completion counters
     Scene* scenes_next;        // temporal mode: per-scene parameters for the next call
     uint32_t* work_start;      // per-scene first work item (S+1), batched plan
+    uint32_t* work_scene;      // scene of every work item, batched plan
     uint32_t* objscene;        // per object scene id (batched only)
     uint32_t* keys[2];
     uint32_t* vals[2];         // object index | owner flags << kFlagShift
@@ -209,6 +210,15 @@ cudaError_t launch_sort_prep(const BpScratch& s, const uint32_t* keys, const uin
 // sub-buckets (keys[1] / vals[1]), local sort of every sub-bucket; the
 // sorted keys end in keys[0] and the entry records in G.smin / G.smax.
 cudaError_t launch_bucket_sort(const BpScratch& s, const SortGather& G, uint32_t spin, cudaStream_t st);
+// Sweep records of the sorted entries (put_record) from their sorted values
+// (object index | owner flags), after the last radix pass: a kernel of its
+// own at full occupancy, several entries' random bound loads in flight per
+// thread.
+cudaError_t launch_gather(const BpScratch& s, const SortGather& G, const uint32_t* vals, const uint32_t* count_ptr,
+                          uint64_t cap, cudaStream_t st);
+// Box bytes (32 per object) above which the broadphase gathers the sweep
+// records in launch_gather instead of in its last radix pass.
+constexpr uint64_t kGatherInPassBytes = 96ull << 20;
 // Per-device set-up of the bucket sort's launch (kernel attributes); called
 // when a handle is created, outside any stream capture.
 cudaError_t bucket_sort_setup();
@@ -397,12 +407,9 @@ __device__ __forceinline__ bool map_work(uint32_t w, const BpScratch& S, const B
         return true;
     }
     if (w >= S.work_start[A.num_scenes]) return false;
-    uint32_t lo = 0, hi = A.num_scenes;  // last s with work_start[s] <= w
-    while (hi - lo > 1) {
-        uint32_t mid = (lo + hi) >> 1;
-        if (S.work_start[mid] <= w) lo = mid;
-        else hi = mid;
-    }
+    // the plan's table (a search over work_start here was a chain of ~12
+    // dependent loads at the start of every CTA of a 4096-scene batch)
+    const uint32_t lo = S.work_scene[w];
     scene = lo;
     wfirst = S.work_start[lo];
     nw = S.work_start[lo + 1] - wfirst;

@@ -54,7 +54,10 @@ __global__ void __launch_bounds__(1024) k_plan(BpScratch S, BpArgs A) {
         }
         __syncthreads();
         uint32_t excl = s_carry + (wid ? s_tot[wid - 1] : 0u) + x - v;
-        if (s < A.num_scenes) S.work_start[s] = excl;
+        if (s < A.num_scenes) {
+            S.work_start[s] = excl;
+            for (uint32_t k = 0; k < v; ++k) S.work_scene[excl + k] = s;  // the scene of each of its items
+        }
         __syncthreads();
         if (threadIdx.x == 1023) s_carry = excl + v;
         __syncthreads();

@@ -188,6 +188,63 @@ __global__ void __launch_bounds__(kThreads, ITEMS <= 8 ? 4 : 2) k_onesweep(BpScr
     }
 }
 
+// Sweep records of the sorted entries.  The last radix pass used to write
+// them from its scatter loop (two CTAs per SM, one entry per thread at a
+// time): the two random 16-byte bound loads per entry then had few peers in
+// flight, and with inputs larger than L2 (the 617 MB of a 4096-scene batch)
+// the pass took three times as long as the others.  Here every thread of a
+// full-occupancy grid issues the loads of kGatherU entries before it stores
+// any record.
+constexpr int kGatherU = 4;
+__global__ void __launch_bounds__(kThreads) k_gather(BpScratch S, SortGather G, const uint32_t* __restrict__ vals,
+                                                    const uint32_t* count_ptr, uint32_t cap) {
+    const uint32_t n = min(*count_ptr, cap);
+    const uint32_t stride = gridDim.x * kThreads;
+    for (uint32_t g0 = blockIdx.x * kThreads + threadIdx.x; g0 < n; g0 += stride * kGatherU) {
+        uint32_t v[kGatherU];
+        float4 lo[kGatherU], hi[kGatherU];
+#pragma unroll
+        for (int u = 0; u < kGatherU; ++u) {
+            const uint32_t g = g0 + u * stride;
+            v[u] = g < n ? __ldcs(vals + g) : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < kGatherU; ++u) {
+            if (g0 + u * stride >= n) continue;
+            const uint32_t obj = v[u] & kObjMask;
+            lo[u] = __ldg(G.mn + obj);
+            if (G.mx) hi[u] = __ldg(G.mx + obj);
+        }
+#pragma unroll
+        for (int u = 0; u < kGatherU; ++u) {
+            const uint32_t g = g0 + u * stride;
+            if (g >= n) continue;
+            const uint32_t obj = v[u] & kObjMask, fl = v[u] >> kFlagShift;
+            if (G.mx) {  // boxes: index and flags ride in the unused w lanes
+                G.smin[g] = make_float4(lo[u].x, lo[u].y, lo[u].z, __uint_as_float(obj));
+                G.smax[g] = make_float4(hi[u].x, hi[u].y, hi[u].z, __uint_as_float(fl));
+            } else {     // spheres: radius in w, index and flags in the second record
+                G.smin[g] = lo[u];
+                G.smax[g] = make_float4(__uint_as_float(obj), __uint_as_float(fl), 0.f, 0.f);
+            }
+        }
+    }
+}
+
+cudaError_t launch_gather(const BpScratch& s, const SortGather& G, const uint32_t* vals, const uint32_t* count_ptr,
+                          uint64_t cap, cudaStream_t st) {
+    static std::once_flag once[kMaxDevices];
+    static int val[kMaxDevices];
+    const int grid = per_device(once, val, [] {
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather, kThreads, 0);
+        return sm_count() * (per_sm > 0 ? per_sm : 1);
+    });
+    const uint32_t c = cap > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)cap;
+    k_gather<<<grid, kThreads, 0, st>>>(s, G, vals, count_ptr, c);
+    return cudaGetLastError();
+}
+
 // Histograms of all passes for a standalone sort.
 template <int PASSES>
 __global__ void __launch_bounds__(kThreads) k_hist(Ctrl* C, const uint32_t* __restrict__ keys, uint32_t n,
