@@ -49,15 +49,25 @@ def test_noalloc_matches_handle_sort_twice(cuda):
 
     radix_sort_noalloc(*dev[0], bits=host[0][2])  # first call on the device: set-up
     torch.cuda.synchronize()
-    free_before = torch.cuda.mem_get_info()[0]
-    torch_before = torch.cuda.memory_allocated()
-    radix_sort_noalloc(*dev[1], bits=host[1][2])
-    radix_sort_noalloc(*dev[0], bits=host[0][2])  # already sorted input: must stay put
-    torch.cuda.synchronize()
+    # no garbage collection inside the window: a cycle of earlier tests'
+    # tensors freed there would move torch's count without our calls
+    import gc
+    gc.collect()
+    gc.disable()
+    try:
+        free_before = torch.cuda.mem_get_info()[0]
+        torch_before = torch.cuda.memory_allocated()
+        radix_sort_noalloc(*dev[1], bits=host[1][2])
+        radix_sort_noalloc(*dev[0], bits=host[0][2])  # already sorted input: must stay put
+        torch.cuda.synchronize()
+        torch_after = torch.cuda.memory_allocated()
+        free_after = torch.cuda.mem_get_info()[0]
+    finally:
+        gc.enable()
     # torch's own allocator saw no allocation; the device's free memory (which
     # other processes on the GPU can also move) is checked as well
-    assert torch.cuda.memory_allocated() == torch_before
-    assert torch.cuda.mem_get_info()[0] == free_before, "device memory changed across no-alloc calls"
+    assert torch_after == torch_before
+    assert free_after == free_before, "device memory changed across no-alloc calls"
 
     for (kd, vd), (ke, ve), (k, v, _) in zip(dev, expect, host):
         assert torch.equal(kd, ke) and torch.equal(vd, ve)
