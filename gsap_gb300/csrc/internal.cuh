@@ -78,10 +78,15 @@ struct Ctrl {
     unsigned long long tests; // sweep: candidate pairs tested (diagnostics)
     unsigned long long iters; // sweep: warp iterations of the candidate loop (diagnostics)
     uint32_t hist[kMaxPasses][256];
+    // first broadphase pass (k_pass0): entries placed so far per digit;
+    // contiguous with hist and zeroed with it (kHistWords words)
+    uint32_t cursor0[256];
     // temporal mode: the key layout computed from this call's input for the
     // next call (committed at the end of the call)
     uint32_t qbits_next, key_bits_next, total_buckets_next, pad_next;
 };
+
+constexpr uint32_t kHistWords = (kMaxPasses + 1) * 256u;
 
 // Per-scene parameters written by the PCA kernel.
 struct Scene {
@@ -210,6 +215,11 @@ cudaError_t launch_sort_prep(const BpScratch& s, const uint32_t* keys, const uin
 // sub-buckets (keys[1] / vals[1]), local sort of every sub-bucket; the
 // sorted keys end in keys[0] and the entry records in G.smin / G.smax.
 cudaError_t launch_bucket_sort(const BpScratch& s, const SortGather& G, uint32_t spin, cudaStream_t st);
+// First radix pass of the broadphase (digit 0 of the projection's entries),
+// not order-preserving: entries of one digit may land in any order, which
+// the first pass of an LSD sort may do (the later passes are stable).
+cudaError_t launch_pass0(const BpScratch& s, const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
+                         uint32_t* vout, const uint32_t* count_ptr, uint64_t cap, cudaStream_t st);
 // Sweep records of the sorted entries (put_record) from their sorted values
 // (object index | owner flags), after the last radix pass: a kernel of its
 // own at full occupancy, several entries' random bound loads in flight per

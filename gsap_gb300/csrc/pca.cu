@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, 
     }
     if (one) {
         if (!temporal)
-            for (int p = 0; p < kMaxPasses; ++p) C->hist[p][tid] = 0u;
+            for (uint32_t k = tid; k < kHistWords; k += 256u) (&C->hist[0][0])[k] = 0u;
         return;
     }
     __syncthreads();
@@ -371,7 +371,7 @@ __global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, 
         reset_counters(C);
         C->epoch = C->epoch + 1u;
     }
-    for (int p = 0; p < kMaxPasses; ++p) C->hist[p][tid] = 0u;
+    for (uint32_t k = tid; k < kHistWords; k += 256u) (&C->hist[0][0])[k] = 0u;
     __syncthreads();
     // quantisation scale of every scene, computed once for all kernels
     const float qf = (float)(1u << s_q);
@@ -504,7 +504,7 @@ __global__ void __launch_bounds__(32 * kFinishWarps) k_pca_finish_batch(BpScratc
         }
     }
     if (!temporal)
-        for (uint32_t k = tid; k < (uint32_t)kMaxPasses * 256u; k += kT) (&C->hist[0][0])[k] = 0u;
+        for (uint32_t k = tid; k < kHistWords; k += kT) (&C->hist[0][0])[k] = 0u;
     const float qf = (float)(1u << q);
     for (uint32_t sc = tid; sc < A.num_scenes; sc += kT) out[sc].q_scale = __fdiv_rn(qf, __ldcg(&out[sc].q_range));
 }
@@ -534,7 +534,7 @@ __global__ void k_reset(BpScratch S) {
         reset_counters(C);
         C->epoch = C->epoch + 1u;
     }
-    for (int p = 0; p < kMaxPasses; ++p) C->hist[p][tid] = 0u;
+    for (uint32_t k = tid; k < kHistWords; k += 256u) (&C->hist[0][0])[k] = 0u;
 }
 
 // Temporal mode, after both branches: the parameters computed from this

@@ -191,6 +191,103 @@ __global__ void __launch_bounds__(kThreads, ITEMS <= 8 ? 4 : 2) k_onesweep(BpScr
     }
 }
 
+// First pass of the broadphase sort (digit 0, the low bits of the quantised
+// lower bound).  The first pass of an LSD sort need not keep the input order
+// within a digit -- nothing earlier ordered the entries, and the later
+// passes are stable -- so a tile needs neither the onesweep's ballot ranking
+// nor its look-back chain: it counts its digits in shared memory, gives
+// every entry a slot in its digit's run of the tile with a shared-memory
+// atomic, stages the tile in digit order, reserves each digit's global range
+// with one atomic on that digit's cursor (ranges start at the digit bases
+// from the projection's histogram; tiles take them in any order) and writes
+// the runs out coalesced.  Entries with equal keys may end in any order; the
+// sweep's pair set does not depend on it.
+template <int ITEMS>
+__global__ void __launch_bounds__(kThreads, 2) k_pass0(BpScratch S, const uint32_t* __restrict__ kin,
+                                                      const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
+                                                      uint32_t* __restrict__ vout, const uint32_t* count_ptr,
+                                                      uint32_t cap) {
+    constexpr int TILE = kThreads * ITEMS;
+    __shared__ uint32_t s_k[TILE];
+    __shared__ uint32_t s_v[TILE];
+    __shared__ uint32_t s_cnt[256];   // the tile's digit counts, then its slot cursors
+    __shared__ uint32_t s_start[256]; // exclusive start of each digit's run in the tile
+    __shared__ uint32_t s_gb[256];    // global position of each digit's run, minus its tile start
+    __shared__ uint32_t s_base[256];  // digit bases of the pass
+    __shared__ uint32_t s_next[256];  // counts of the next digit over this CTA's tiles
+    __shared__ uint32_t s_scan[8];
+    const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    Ctrl* C = S.ctrl;
+    const uint32_t n = min(*count_ptr, cap);
+    const uint32_t ntiles = (n + TILE - 1) / TILE;
+    s_base[tid] = cta_excl_scan256(C->hist[0][tid], s_scan);
+    s_next[tid] = 0u;
+    for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const uint32_t tbase = t * TILE;
+        const uint32_t wb = tbase + wid * 32 * ITEMS;
+        uint32_t key[ITEMS], val[ITEMS];
+        s_cnt[tid] = 0u;
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            const uint32_t idx = wb + k * 32 + lane;
+            key[k] = idx < n ? __ldcs(kin + idx) : 0u;
+            val[k] = idx < n ? __ldcs(vin + idx) : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k)
+            if (wb + k * 32 + lane < n) atomicAdd(&s_cnt[key[k] & 255u], 1u);
+        __syncthreads();
+        const uint32_t cnt = s_cnt[tid];
+        const uint32_t st = cta_excl_scan256(cnt, s_scan);  // (has its own barriers)
+        s_start[tid] = st;
+        // this tile's range of the digit (any order among tiles)
+        const uint32_t g = cnt ? atomicAdd(&C->cursor0[tid], cnt) : 0u;
+        s_gb[tid] = s_base[tid] + g - st;
+        s_cnt[tid] = st;  // slot cursors
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+            if (wb + k * 32 + lane < n) {
+                const uint32_t lp = atomicAdd(&s_cnt[key[k] & 255u], 1u);
+                s_k[lp] = key[k];
+                s_v[lp] = val[k];
+                atomicAdd(&s_next[(key[k] >> 8) & 255u], 1u);
+            }
+        }
+        __syncthreads();
+        const uint32_t tn = min((uint32_t)TILE, n - tbase);
+        for (uint32_t i = tid; i < tn; i += kThreads) {
+            const uint32_t kk = s_k[i];
+            const uint32_t gp = s_gb[kk & 255u] + i;
+            if (gp >= n) {  // cannot happen with consistent counts; never write out of range
+                atomicOr(&C->error, kErrInternal);
+                continue;
+            }
+            kout[gp] = kk;
+            vout[gp] = s_v[i];
+        }
+        __syncthreads();  // s_k / s_v / s_cnt are reused by the next tile
+    }
+    __syncthreads();
+    const uint32_t c = s_next[tid];
+    if (c) atomicAdd(&C->hist[1][tid], c);
+}
+
+cudaError_t launch_pass0(const BpScratch& s, const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
+                         uint32_t* vout, const uint32_t* count_ptr, uint64_t cap, cudaStream_t st) {
+    static std::once_flag once[kMaxDevices];
+    static int val[kMaxDevices];
+    const int grid = per_device(once, val, [] {
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pass0<kSortItems>, kThreads, 0);
+        return sm_count() * (per_sm > 0 ? per_sm : 1);
+    });
+    const uint32_t c = cap > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)cap;
+    k_pass0<kSortItems><<<grid, kThreads, 0, st>>>(s, kin, vin, kout, vout, count_ptr, c);
+    return cudaGetLastError();
+}
+
 // Sweep records of the sorted entries.  The last radix pass used to write
 // them from its scatter loop (two CTAs per SM, one entry per thread at a
 // time): the two random 16-byte bound loads per entry then had few peers in
@@ -270,7 +367,7 @@ __global__ void __launch_bounds__(kThreads) k_hist(Ctrl* C, const uint32_t* __re
 // Counter reset + new epoch for a standalone sort.
 __global__ void k_sort_reset(Ctrl* C, uint32_t n, uint32_t* count_slot) {
     uint32_t t = threadIdx.x;
-    for (int p = 0; p < kMaxPasses; ++p) C->hist[p][t] = 0u;
+    for (uint32_t k = t; k < kHistWords; k += 256u) (&C->hist[0][0])[k] = 0u;
     if (t == 0) {
         for (int p = 0; p < kMaxPasses + 4; ++p) C->tile_ctr[p] = 0;
         C->epoch = C->epoch + 1u;
