@@ -51,6 +51,7 @@ __device__ __forceinline__ uint32_t block_sum256(uint32_t v, uint32_t* s_w) {
 }
 
 __global__ void __launch_bounds__(256) k_subsum(BpScratch S) {
+    pdl_wait();
     __shared__ uint32_t s_w[8];
     const SubLayout L = sub_layout(S.ctrl);
     const uint32_t t = blockIdx.x;
@@ -73,6 +74,7 @@ __global__ void __launch_bounds__(256) k_subsum(BpScratch S) {
 // Exclusive offsets of the sub-buckets (substart[0..count]) and the counts
 // back to zero.
 __global__ void __launch_bounds__(256) k_subscan(BpScratch S) {
+    pdl_wait();
     __shared__ uint32_t s_w[8];
     const SubLayout L = sub_layout(S.ctrl);
     const uint32_t t = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -120,6 +122,7 @@ __global__ void __launch_bounds__(256) k_subscan(BpScratch S) {
 
 // Every entry into its sub-bucket (cursor = the count, from zero).
 __global__ void __launch_bounds__(256) k_subscatter(BpScratch S) {
+    pdl_wait();
     const Ctrl* C = S.ctrl;
     const uint32_t E = (uint32_t)min((uint64_t)C->entry_count, S.entry_cap);
     const SubLayout L = sub_layout(C);
@@ -393,6 +396,7 @@ __device__ void sort_segment_global(BsShared& B, const BpScratch& S, const SortG
 }
 
 __global__ void __launch_bounds__(kBsThreads, 1) k_subsort(BpScratch S, SortGather G) {
+    pdl_wait();
     extern __shared__ __align__(16) unsigned char bs_smem[];
     BsShared& B = *reinterpret_cast<BsShared*>(bs_smem);
     const Ctrl* C = S.ctrl;
@@ -460,10 +464,10 @@ cudaError_t bucket_sort_setup() {
 
 cudaError_t launch_bucket_sort(const BpScratch& s, const SortGather& G, uint32_t spin, cudaStream_t st) {
     (void)spin;
-    k_subsum<<<kSubScanTiles, 256, 0, st>>>(s);
-    k_subscan<<<kSubScanTiles, 256, 0, st>>>(s);
-    k_subscatter<<<sm_count() * 8, 256, 0, st>>>(s);
-    k_subsort<<<subsort_grid(), kBsThreads, sizeof(BsShared), st>>>(s, G);
+    launch_pdl(k_subsum, kSubScanTiles, 256, 0, st, s);
+    launch_pdl(k_subscan, kSubScanTiles, 256, 0, st, s);
+    launch_pdl(k_subscatter, sm_count() * 8, 256, 0, st, s);
+    launch_pdl(k_subsort, subsort_grid(), kBsThreads, sizeof(BsShared), st, s, G);
     return cudaGetLastError();
 }
 

@@ -72,6 +72,7 @@ __device__ __forceinline__ uint32_t warp_lookback1(uint64_t* status, uint32_t t,
 template <int MODE>
 __global__ void __launch_bounds__(kThreads) k_scan(BpScratch S, uint32_t* in, uint32_t* out, int32_t* entries,
                                                    uint64_t entry_cap, uint32_t n, int slot, uint32_t spin) {
+    pdl_wait();
     __shared__ uint32_t s_w[8];
     __shared__ uint32_t s_tile, s_excl;
     const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -180,6 +181,7 @@ __device__ __forceinline__ uint32_t cta_sum256(uint32_t v, uint32_t* s_w) {
 }
 
 __global__ void __launch_bounds__(kThreads) k_rowsum(const uint32_t* __restrict__ in, uint32_t* tsum, uint32_t n) {
+    pdl_wait();
     __shared__ uint32_t s_w[kThreads / 32];
     const uint32_t b = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     uint32_t sum = 0;
@@ -203,6 +205,7 @@ __global__ void __launch_bounds__(kThreads) k_rowsum(const uint32_t* __restrict_
 constexpr uint32_t kDirectTiles = 512;
 
 __global__ void __launch_bounds__(1024) k_tilescan(uint32_t* tsum, uint32_t ntiles) {
+    pdl_wait();
     __shared__ uint32_t s_w[32];
     __shared__ uint32_t s_carry;
     const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -241,6 +244,7 @@ __device__ __forceinline__ bool scatter_zeroes(uint64_t pairs, uint32_t n) { ret
 __global__ void __launch_bounds__(kThreads) k_rowscan(uint32_t* in, uint32_t* out, const uint32_t* __restrict__ tsum,
                                                       uint32_t n, int scanned, const Ctrl* __restrict__ C,
                                                       uint64_t pair_cap) {
+    pdl_wait();
     const bool zero = !scatter_zeroes(min((uint64_t)C->pair_count, pair_cap), n);
     __shared__ uint32_t s_w[kThreads / 32];
     const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -318,6 +322,7 @@ __global__ void __launch_bounds__(kThreads) k_rowscan(uint32_t* in, uint32_t* ou
 // back to zero; the other rows' counters are zero already.
 __global__ void __launch_bounds__(kThreads) k_scatter(BpScratch S, const uint2* __restrict__ in, uint64_t in_cap,
                                                       uint2* out, uint64_t out_cap, int both, uint32_t n) {
+    pdl_wait();
     const uint64_t P = min((uint64_t)S.ctrl->pair_count, in_cap);
     const bool zero = scatter_zeroes(P, n);
     const uint32_t* off = S.rowoff;
@@ -378,6 +383,7 @@ constexpr int kLongRow = 1024;       // per-warp shared-memory sort limit
 constexpr uint32_t kRankTile = 2048;
 __global__ void __launch_bounds__(kThreads) k_rank(BpScratch S, const uint2* __restrict__ grp, uint64_t grp_cap,
                                                    uint32_t n, uint2* out, uint64_t out_cap) {
+    pdl_wait();
     __shared__ uint2 s_p[kRankTile + kRankRow];
     const uint32_t P = (uint32_t)min((uint64_t)S.rowoff[n], grp_cap);  // grouped entries
     const uint32_t ntiles = (P + kRankTile - 1) / kRankTile;
@@ -409,6 +415,7 @@ __global__ void __launch_bounds__(kThreads) k_rank(BpScratch S, const uint2* __r
 // kLongRow, rank placement by the warp beyond (pathological overlap).
 __global__ void __launch_bounds__(kThreads) k_rowsort_long(BpScratch S, const uint2* __restrict__ grp, uint2* out,
                                                            uint64_t out_cap) {
+    pdl_wait();
     __shared__ uint32_t s_all[kThreads / 32][kLongRow];
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     uint32_t* s = s_all[wid];
@@ -454,15 +461,16 @@ cudaError_t launch_canonical(const BpScratch& s, uint32_t n, const uint2* in_pai
                              uint32_t spin, cudaStream_t st) {
     const int grid = sm_count() * 4;
     const uint32_t ntiles = (n + kScanTile - 1) / kScanTile;
-    k_rowsum<<<ntiles, kThreads, 0, st>>>(s.rowcnt, s.tile_sums, n);
+    launch_pdl(k_rowsum, ntiles, kThreads, 0, st, s.rowcnt, s.tile_sums, n);
     const int scanned = ntiles > kDirectTiles ? 1 : 0;
-    if (scanned) k_tilescan<<<1, 1024, 0, st>>>(s.tile_sums, ntiles);
-    k_rowscan<<<ntiles, kThreads, 0, st>>>(s.rowcnt, s.rowoff, s.tile_sums, n, scanned, s.ctrl, in_cap);
+    if (scanned) launch_pdl(k_tilescan, 1, 1024, 0, st, s.tile_sums, ntiles);
+    launch_pdl(k_rowscan, ntiles, kThreads, 0, st, s.rowcnt, s.rowoff, s.tile_sums, n, scanned, s.ctrl, in_cap);
     const uint64_t grp_cap = 2 * s.pair_cap_internal;
-    k_scatter<<<sm_count() * 16, kThreads, 0, st>>>(s, in_pairs, in_cap, s.grp_pairs, grp_cap, both, n);
-    k_rank<<<sm_count() * 8, kThreads, 0, st>>>(s, s.grp_pairs, grp_cap, n, out_pairs, out_cap);
-    k_rowsort_long<<<sm_count() * 2, kThreads, 0, st>>>(s, s.grp_pairs, out_pairs, out_cap);
-    if (both && entries) k_scan<1><<<grid, kThreads, 0, st>>>(s, s.rowoff, nullptr, entries, entry_cap, n, 6, spin);
+    launch_pdl(k_scatter, sm_count() * 16, kThreads, 0, st, s, in_pairs, in_cap, s.grp_pairs, grp_cap, both, n);
+    launch_pdl(k_rank, sm_count() * 8, kThreads, 0, st, s, s.grp_pairs, grp_cap, n, out_pairs, out_cap);
+    launch_pdl(k_rowsort_long, sm_count() * 2, kThreads, 0, st, s, s.grp_pairs, out_pairs, out_cap);
+    if (both && entries) launch_pdl(k_scan<1>, grid, kThreads, 0, st, s, s.rowoff, nullptr, entries, entry_cap, n, 6,
+            spin);
     return cudaGetLastError();
 }
 

@@ -20,6 +20,31 @@ int per_device(std::once_flag (&once)[kMaxDevices], int (&val)[kMaxDevices], F c
     return val[dev];
 }
 
+// Pipeline kernels are launched with programmatic stream serialisation: a
+// kernel's CTAs may be scheduled as soon as every CTA of the kernel before it
+// in the stream has exited, without waiting for that grid's completion to be
+// processed, so the launch latency of each link of the chain overlaps the
+// end of the previous one.  Every kernel launched this way begins with
+// pdl_wait(), which waits (in hardware) until the previous kernel has
+// completed and its writes are visible, before any other statement.  So a
+// kernel still starts its work only after all earlier ones have finished,
+// as under plain stream order.
+template <typename... P, typename... A>
+inline cudaError_t launch_pdl(void (*kernel)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                              A&&... args) {
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<A&&>(args)...);
+}
+
 constexpr int kChunk = 4096;          // objects per PCA / projection work item
 // Calls of at most kPcaSmallWork work items run kPcaSplitSmall PCA CTAs per
 // item (one object per thread), each with its own partial.
@@ -279,6 +304,12 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
     return m;
 }
+// First statement of every kernel launched by launch_pdl: wait until the
+// previous kernel of the stream has completed and its writes are visible.
+// (No kernel signals its dependents early: a dependent scheduled while the
+// current kernel still runs lands its CTAs unevenly on the SMs, which cost
+// the grid-stride kernels more than the earlier start gained.)
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ uint64_t lb_word(uint32_t tag, uint64_t flag, uint32_t val) {
     return ((uint64_t)tag << 32) | flag | (uint64_t)(val & kValMask);
 }

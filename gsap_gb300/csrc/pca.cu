@@ -23,6 +23,7 @@ namespace gsap {
 // Batched plan: first work item of every scene (one CTA, sequential scan in
 // 1024-scene blocks).
 __global__ void __launch_bounds__(1024) k_plan(BpScratch S, BpArgs A) {
+    pdl_wait();
     __shared__ uint32_t s_tot[32];
     __shared__ uint32_t s_carry;
     if (threadIdx.x == 0) s_carry = 0;
@@ -88,6 +89,7 @@ __device__ __forceinline__ void pilot_of(const BpArgs& A, uint32_t sb, uint32_t 
 // items spread over more SMs (kPcaSplitSmall), large calls take one CTA per
 // item.
 __global__ void __launch_bounds__(kThreads) k_pca(BpScratch S, BpArgs A, uint32_t split) {
+    pdl_wait();
     __shared__ float s_red[kThreads / 32][2 * kPcaQ + 3];
     const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     uint32_t scene, b, e, wfirst, nw;
@@ -212,6 +214,7 @@ __device__ __forceinline__ void reset_counters(Ctrl* C) {
 
 __global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, uint64_t entry_cap, int temporal,
                                                          uint32_t split) {
+    pdl_wait();
     Scene* const out = temporal ? S.scenes_next : S.scenes;
     __shared__ uint32_t s_flag;
     const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -390,6 +393,7 @@ constexpr int kFinishWarps = 16;
 constexpr int kFinishScenes = 32;
 __global__ void __launch_bounds__(32 * kFinishWarps) k_pca_finish_batch(BpScratch S, BpArgs A, uint64_t entry_cap,
                                                                        int temporal, uint32_t split) {
+    pdl_wait();
     __shared__ SceneSums s_z[kFinishScenes];
     Scene* const out = temporal ? S.scenes_next : S.scenes;
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -510,24 +514,25 @@ __global__ void __launch_bounds__(32 * kFinishWarps) k_pca_finish_batch(BpScratc
 }
 
 cudaError_t launch_plan(const BpScratch& s, const BpArgs& a, cudaStream_t st) {
-    k_plan<<<1, 1024, 0, st>>>(s, a);
+    launch_pdl(k_plan, 1, 1024, 0, st, s, a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_pca(const BpScratch& s, const BpArgs& a, cudaStream_t st, int temporal) {
     const uint32_t split = a.num_work <= kPcaSmallWork ? kPcaSplitSmall : 1u;
-    k_pca<<<a.num_work * split, kThreads, 0, st>>>(s, a, split);
+    launch_pdl(k_pca, a.num_work * split, kThreads, 0, st, s, a, split);
     if (a.num_scenes > 1)
-        k_pca_finish_batch<<<(a.num_scenes + kFinishScenes - 1) / kFinishScenes, 32 * kFinishWarps, 0, st>>>(
-            s, a, s.entry_cap, temporal, split);
+        launch_pdl(k_pca_finish_batch, (a.num_scenes + kFinishScenes - 1) / kFinishScenes, 32 * kFinishWarps, 0, st,
+                s, a, s.entry_cap, temporal, split);
     else
-        k_pca_finish<<<1, kThreads, 0, st>>>(s, a, s.entry_cap, temporal, split);
+        launch_pdl(k_pca_finish, 1, kThreads, 0, st, s, a, s.entry_cap, temporal, split);
     return cudaGetLastError();
 }
 
 // Temporal mode, main branch: the counter resets that the finish does in the
 // plain pipeline.
 __global__ void k_reset(BpScratch S) {
+    pdl_wait();
     Ctrl* C = S.ctrl;
     const uint32_t tid = threadIdx.x;
     if (tid == 0) {
@@ -540,6 +545,7 @@ __global__ void k_reset(BpScratch S) {
 // Temporal mode, after both branches: the parameters computed from this
 // call's input become the ones the next call uses.
 __global__ void k_commit(BpScratch S, uint32_t num_scenes) {
+    pdl_wait();
     // the records as 8-byte words, one per thread (coalesced)
     static_assert(sizeof(Scene) % 8 == 0, "Scene is copied in 8-byte words");
     const uint64_t words = (uint64_t)num_scenes * (sizeof(Scene) / 8);
@@ -554,13 +560,13 @@ __global__ void k_commit(BpScratch S, uint32_t num_scenes) {
 }
 
 cudaError_t launch_reset(const BpScratch& s, cudaStream_t st) {
-    k_reset<<<1, 256, 0, st>>>(s);
+    launch_pdl(k_reset, 1, 256, 0, st, s);
     return cudaGetLastError();
 }
 
 cudaError_t launch_commit(const BpScratch& s, uint32_t num_scenes, cudaStream_t st) {
     const uint64_t words = (uint64_t)num_scenes * (sizeof(Scene) / 8);
-    k_commit<<<(unsigned)((words + 255) / 256), 256, 0, st>>>(s, num_scenes);
+    launch_pdl(k_commit, (unsigned)((words + 255) / 256), 256, 0, st, s, num_scenes);
     return cudaGetLastError();
 }
 

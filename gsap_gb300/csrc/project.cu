@@ -53,6 +53,7 @@ constexpr int kProjStage = 128;          // entries of one item staged per warp
 // (global atomics; sub_layout in internal.cuh).
 template <int PASSES, int ITEMS>
 __global__ void __launch_bounds__(kThreads, 4) k_project(BpScratch S, BpArgs A) {
+    pdl_wait();
     constexpr int kProjItems = ITEMS;
     constexpr int kProjHalf = kThreads * kProjItems;  // objects per CTA
     constexpr int kProjSplit = kChunk / kProjHalf;    // CTAs per work item
@@ -201,14 +202,14 @@ __global__ void __launch_bounds__(kThreads, 4) k_project(BpScratch S, BpArgs A) 
 cudaError_t launch_project(const BpScratch& s, const BpArgs& a, int passes, cudaStream_t st) {
     if (a.num_work <= kProjSmallWork) {
         constexpr int kSplit = kChunk / (kThreads * kProjItemsSmall);
-        if (passes == 0) k_project<0, kProjItemsSmall><<<a.num_work * kSplit, kThreads, 0, st>>>(s, a);
-        else if (passes == 3) k_project<3, kProjItemsSmall><<<a.num_work * kSplit, kThreads, 0, st>>>(s, a);
-        else k_project<4, kProjItemsSmall><<<a.num_work * kSplit, kThreads, 0, st>>>(s, a);
+        if (passes == 0) launch_pdl(k_project<0, kProjItemsSmall>, a.num_work * kSplit, kThreads, 0, st, s, a);
+        else if (passes == 3) launch_pdl(k_project<3, kProjItemsSmall>, a.num_work * kSplit, kThreads, 0, st, s, a);
+        else launch_pdl(k_project<4, kProjItemsSmall>, a.num_work * kSplit, kThreads, 0, st, s, a);
     } else {
         constexpr int kSplit = kChunk / (kThreads * kProjItemsLarge);
-        if (passes == 0) k_project<0, kProjItemsLarge><<<a.num_work * kSplit, kThreads, 0, st>>>(s, a);
-        else if (passes == 3) k_project<3, kProjItemsLarge><<<a.num_work * kSplit, kThreads, 0, st>>>(s, a);
-        else k_project<4, kProjItemsLarge><<<a.num_work * kSplit, kThreads, 0, st>>>(s, a);
+        if (passes == 0) launch_pdl(k_project<0, kProjItemsLarge>, a.num_work * kSplit, kThreads, 0, st, s, a);
+        else if (passes == 3) launch_pdl(k_project<3, kProjItemsLarge>, a.num_work * kSplit, kThreads, 0, st, s, a);
+        else launch_pdl(k_project<4, kProjItemsLarge>, a.num_work * kSplit, kThreads, 0, st, s, a);
     }
     return cudaGetLastError();
 }

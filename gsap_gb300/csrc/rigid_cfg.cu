@@ -63,6 +63,7 @@ __device__ __forceinline__ void ff_add(float& hi, float& lo, float d) {
 
 __global__ void k_integrate_cfg(float4* pos, float4* pos_lo, float4* quat, float4* lin, const float4* ang,
                                 CfgParams p, int n) {
+    pdl_wait();
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= n) return;
     float4 v = lin[b];
@@ -95,6 +96,7 @@ __global__ void k_integrate_cfg(float4* pos, float4* pos_lo, float4* quat, float
 __global__ void k_place_cfg(const float4* quat, const float4* lin, const float4* ang, const int* shape,
                             const int* pstart, const int* p_body, const float4* ref_pos, float4* p_rel,
                             float4* p_vel, int np) {
+    pdl_wait();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= np) return;
     int b = p_body[i];
@@ -111,6 +113,7 @@ __global__ void k_place_cfg(const float4* quat, const float4* lin, const float4*
 // absolute particle positions (readback only): hi + (lo + r)
 __global__ void k_abs_pos(const float4* pos, const float4* pos_lo, const int* p_body, const float4* p_rel,
                           float4* p_pos, int np) {
+    pdl_wait();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= np) return;
     const int b = p_body[i];
@@ -120,6 +123,7 @@ __global__ void k_abs_pos(const float4* pos, const float4* pos_lo, const int* p_
 
 __global__ void k_body_aabb(const float4* pos, const float4* pos_lo, const float4* p_rel, const int* pstart,
                             const int* npart, float4* bmin, float4* bmax, int n) {
+    pdl_wait();
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= n) return;
     int s = pstart[b], m = npart[b];
@@ -156,6 +160,7 @@ __global__ void __launch_bounds__(256) k_forces_cfg(const float4* __restrict__ p
                                                     const int* pstart, const int* npart, const uint2* body_pairs,
                                                     const uint32_t* rowoff, uint64_t pair_cap, CfgParams p,
                                                     float4* p_force, int np) {
+    pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t ncontact = 0;  // particle-particle contacts of particle i (walls not counted)
     if (i < np) {
@@ -219,6 +224,7 @@ __device__ __forceinline__ void ts_add(float& s, float& c, float x) {
 __global__ void k_update_cfg(float4* lin, float4* ang, const float4* quat, const float* inv_mass, const int* shape,
                              const int* pstart, const int* npart, const float4* ref_pos, const float4* shape_inv,
                              const float4* p_force, CfgParams p, int n) {
+    pdl_wait();
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= n) return;
     float3 R[3];
@@ -257,23 +263,24 @@ static inline int gr(int n) { return n <= 0 ? 1 : (n + 255) / 256; }
 
 cudaError_t rb_integrate_cfg(float4* pos, float4* pos_lo, float4* quat, float4* lin, const float4* ang,
                              const CfgParams& p, int n, cudaStream_t st) {
-    if (n > 0) k_integrate_cfg<<<gr(n), 256, 0, st>>>(pos, pos_lo, quat, lin, ang, p, n);
+    if (n > 0) launch_pdl(k_integrate_cfg, gr(n), 256, 0, st, pos, pos_lo, quat, lin, ang, p, n);
     return cudaGetLastError();
 }
 cudaError_t rb_place_cfg(const float4* quat, const float4* lin, const float4* ang, const int* shape,
                          const int* pstart, const int* p_body, const float4* ref_pos, float4* p_rel, float4* p_vel,
                          int np, cudaStream_t st) {
-    if (np > 0) k_place_cfg<<<gr(np), 256, 0, st>>>(quat, lin, ang, shape, pstart, p_body, ref_pos, p_rel, p_vel, np);
+    if (np > 0) launch_pdl(k_place_cfg, gr(np), 256, 0, st, quat, lin, ang, shape, pstart, p_body, ref_pos, p_rel,
+            p_vel, np);
     return cudaGetLastError();
 }
 cudaError_t rb_abs_pos(const float4* pos, const float4* pos_lo, const int* p_body, const float4* p_rel, float4* p_pos,
                        int np, cudaStream_t st) {
-    if (np > 0) k_abs_pos<<<gr(np), 256, 0, st>>>(pos, pos_lo, p_body, p_rel, p_pos, np);
+    if (np > 0) launch_pdl(k_abs_pos, gr(np), 256, 0, st, pos, pos_lo, p_body, p_rel, p_pos, np);
     return cudaGetLastError();
 }
 cudaError_t rb_body_aabb(const float4* pos, const float4* pos_lo, const float4* p_rel, const int* pstart,
                          const int* npart, float4* bmin, float4* bmax, int n, cudaStream_t st) {
-    if (n > 0) k_body_aabb<<<gr(n), 256, 0, st>>>(pos, pos_lo, p_rel, pstart, npart, bmin, bmax, n);
+    if (n > 0) launch_pdl(k_body_aabb, gr(n), 256, 0, st, pos, pos_lo, p_rel, pstart, npart, bmin, bmax, n);
     return cudaGetLastError();
 }
 cudaError_t rb_forces_cfg(const float4* pos, const float4* pos_lo, const float4* p_rel, const float4* p_vel,
@@ -281,16 +288,16 @@ cudaError_t rb_forces_cfg(const float4* pos, const float4* pos_lo, const float4*
                           const uint32_t* rowoff, uint64_t pair_cap, const CfgParams& p, float4* p_force, int np,
                           cudaStream_t st) {
     if (np > 0)
-        k_forces_cfg<<<gr(np), 256, 0, st>>>(pos, pos_lo, p_rel, p_vel, p_body, pstart, npart, body_pairs, rowoff,
-                                             pair_cap, p, p_force, np);
+        launch_pdl(k_forces_cfg, gr(np), 256, 0, st, pos, pos_lo, p_rel, p_vel, p_body, pstart, npart, body_pairs,
+                rowoff, pair_cap, p, p_force, np);
     return cudaGetLastError();
 }
 cudaError_t rb_update_cfg(float4* lin, float4* ang, const float4* quat, const float* inv_mass, const int* shape,
                           const int* pstart, const int* npart, const float4* ref_pos, const float4* shape_inv,
                           const float4* p_force, const CfgParams& p, int n, cudaStream_t st) {
     if (n > 0)
-        k_update_cfg<<<gr(n), 256, 0, st>>>(lin, ang, quat, inv_mass, shape, pstart, npart, ref_pos, shape_inv, p_force,
-                                            p, n);
+        launch_pdl(k_update_cfg, gr(n), 256, 0, st, lin, ang, quat, inv_mass, shape, pstart, npart, ref_pos,
+                shape_inv, p_force, p, n);
     return cudaGetLastError();
 }
 

@@ -14,6 +14,7 @@
 // placement runs one thread per particle (coalesced float4 stores) instead
 // of one thread per body looping over its particles; the arithmetic per
 // particle is unchanged.
+#include "internal.cuh"
 #include "rigid.cuh"
 
 namespace gsap {
@@ -71,6 +72,7 @@ using namespace rbref;
 
 __global__ void k_integrate_ref(float4* pos, float4* quat, float4* lin, float4* ang, float dt, int n, float gy,
                                 int floor_clamp) {
+    pdl_wait();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     f4 lv = add(ld(lin + i), mul(mk(0.0f, gy, 0.0f, 0.0f), dt));
@@ -96,6 +98,7 @@ __global__ void k_integrate_ref(float4* pos, float4* quat, float4* lin, float4* 
 __global__ void k_place_ref(const float4* pos, const float4* quat, const float4* lin, const float4* ang,
                             const int* shape, const int* pstart, const int* p_body, const float4* ref_pos,
                             const float* ref_mass, float4* p_pos, float4* p_vel, float* p_mass, int np) {
+    pdl_wait();
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= np) return;
     int b = p_body[p];
@@ -112,6 +115,7 @@ __global__ void k_place_ref(const float4* pos, const float4* quat, const float4*
 __global__ void k_place_ref_body(const float4* pos, const float4* quat, const float4* lin, const float4* ang,
                                  const int* shape, const int* pstart, const int* npart, const float4* ref_pos,
                                  const float* ref_mass, float4* p_pos, float4* p_vel, float* p_mass, int n) {
+    pdl_wait();
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= n) return;
     int s = pstart[b];
@@ -128,6 +132,7 @@ __global__ void k_place_ref_body(const float4* pos, const float4* quat, const fl
 }
 
 __global__ void k_prepare_ref(const float4* quat, const int* shape, const float4* shape_inv, float4* inv_out, int n) {
+    pdl_wait();
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= n) return;
     f4 r[3], rt[3], is[3], t[3], o[3];
@@ -144,6 +149,7 @@ __global__ void k_prepare_ref(const float4* quat, const int* shape, const float4
 
 __global__ void k_clear_force_ref(const float4* p_pos, const float4* p_vel, const float* p_mass, float4* p_force,
                                   float sp, float dp, int np, float dt) {
+    pdl_wait();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= np) return;
     float dt2i = 1.f / (dt * dt), dti = 1.f / dt;
@@ -174,6 +180,7 @@ __global__ void k_pair_force_ref(const float4* p_pos, const float4* p_vel, const
                                  int num_pairs, int num_entries, const unsigned long long* d_num_pairs2,
                                  const uint32_t* d_num_entries, const float* p_mass, float sp, float dp,
                                  float4* p_force, float dt, int quirk, int pair_cap, int entry_cap) {
+    pdl_wait();
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (d_num_entries) num_entries = (int)min(*d_num_entries, (uint32_t)entry_cap);
     if (d_num_pairs2) num_pairs = (int)min(2ull * *d_num_pairs2, (unsigned long long)pair_cap);
@@ -212,6 +219,7 @@ __global__ void k_update_velocity_ref(float4* lin, float4* ang, const float4* qu
                                       const float4* inv_inertia, const int* shape, const int* pstart,
                                       const int* npart, const float4* ref_pos, const float4* p_force, int n,
                                       float dt, float max_lin_vel, int cap, int torque_quirk) {
+    pdl_wait();
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= n) return;
     f4 q = ld(quat + b);
@@ -251,7 +259,7 @@ static inline int grid_for(int n) { return n <= 0 ? 1 : (n + 255) / 256; }
 
 cudaError_t rb_integrate_ref(float4* pos, float4* quat, float4* lin, float4* ang, float dt, int n, float gy,
                              int floor_clamp, cudaStream_t st) {
-    if (n > 0) k_integrate_ref<<<grid_for(n), 256, 0, st>>>(pos, quat, lin, ang, dt, n, gy, floor_clamp);
+    if (n > 0) launch_pdl(k_integrate_ref, grid_for(n), 256, 0, st, pos, quat, lin, ang, dt, n, gy, floor_clamp);
     return cudaGetLastError();
 }
 cudaError_t rb_place_ref(const float4* pos, const float4* quat, const float4* lin, const float4* ang,
@@ -260,22 +268,23 @@ cudaError_t rb_place_ref(const float4* pos, const float4* quat, const float4* li
                          int n, int np, cudaStream_t st) {
     if (p_body) {
         if (np > 0)
-            k_place_ref<<<grid_for(np), 256, 0, st>>>(pos, quat, lin, ang, shape, pstart, p_body, ref_pos, ref_mass,
-                                                      p_pos, p_vel, p_mass, np);
+            launch_pdl(k_place_ref, grid_for(np), 256, 0, st, pos, quat, lin, ang, shape, pstart, p_body, ref_pos,
+                    ref_mass, p_pos, p_vel, p_mass, np);
     } else if (n > 0) {
-        k_place_ref_body<<<grid_for(n), 256, 0, st>>>(pos, quat, lin, ang, shape, pstart, npart, ref_pos, ref_mass,
-                                                       p_pos, p_vel, p_mass, n);
+        launch_pdl(k_place_ref_body, grid_for(n), 256, 0, st, pos, quat, lin, ang, shape, pstart, npart, ref_pos,
+                ref_mass, p_pos, p_vel, p_mass, n);
     }
     return cudaGetLastError();
 }
 cudaError_t rb_prepare_ref(const float4* quat, const int* shape, const float4* shape_inv, float4* inv_out, int n,
                            cudaStream_t st) {
-    if (n > 0) k_prepare_ref<<<grid_for(n), 256, 0, st>>>(quat, shape, shape_inv, inv_out, n);
+    if (n > 0) launch_pdl(k_prepare_ref, grid_for(n), 256, 0, st, quat, shape, shape_inv, inv_out, n);
     return cudaGetLastError();
 }
 cudaError_t rb_clear_force_ref(const float4* p_pos, const float4* p_vel, const float* p_mass, float4* p_force,
                                float sp, float dp, int np, float dt, cudaStream_t st) {
-    if (np > 0) k_clear_force_ref<<<grid_for(np), 256, 0, st>>>(p_pos, p_vel, p_mass, p_force, sp, dp, np, dt);
+    if (np > 0) launch_pdl(k_clear_force_ref, grid_for(np), 256, 0, st, p_pos, p_vel, p_mass, p_force, sp, dp, np,
+            dt);
     return cudaGetLastError();
 }
 cudaError_t rb_pair_force_ref(const float4* p_pos, const float4* p_vel, const int2* pairs, const int* entries,
@@ -284,8 +293,8 @@ cudaError_t rb_pair_force_ref(const float4* p_pos, const float4* p_vel, const in
                               float dt, int quirk, int pair_cap, cudaStream_t st) {
     int g = d_ne ? max_entries : num_entries;
     if (g > 0)
-        k_pair_force_ref<<<grid_for(g), 256, 0, st>>>(p_pos, p_vel, pairs, entries, num_pairs, num_entries, d_np2,
-                                                      d_ne, p_mass, sp, dp, p_force, dt, quirk, pair_cap, g);
+        launch_pdl(k_pair_force_ref, grid_for(g), 256, 0, st, p_pos, p_vel, pairs, entries, num_pairs, num_entries,
+                d_np2, d_ne, p_mass, sp, dp, p_force, dt, quirk, pair_cap, g);
     return cudaGetLastError();
 }
 cudaError_t rb_update_velocity_ref(float4* lin, float4* ang, const float4* quat, const float* inv_mass,
@@ -293,9 +302,8 @@ cudaError_t rb_update_velocity_ref(float4* lin, float4* ang, const float4* quat,
                                    const float4* ref_pos, const float4* p_force, int n, float dt, float max_lin_vel,
                                    int cap, int torque_quirk, cudaStream_t st) {
     if (n > 0)
-        k_update_velocity_ref<<<grid_for(n), 256, 0, st>>>(lin, ang, quat, inv_mass, inv_inertia, shape, pstart,
-                                                           npart, ref_pos, p_force, n, dt, max_lin_vel, cap,
-                                                           torque_quirk);
+        launch_pdl(k_update_velocity_ref, grid_for(n), 256, 0, st, lin, ang, quat, inv_mass, inv_inertia, shape,
+                pstart, npart, ref_pos, p_force, n, dt, max_lin_vel, cap, torque_quirk);
     return cudaGetLastError();
 }
 

@@ -53,6 +53,7 @@ __global__ void __launch_bounds__(kThreads, ITEMS <= 8 ? 4 : 2) k_onesweep(BpScr
                                                        uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
                                                        const uint32_t* count_ptr, uint32_t cap, int pass,
                                                        uint32_t spin, SortGather G, int count_next, int fmode) {
+    pdl_wait();
     constexpr int TILE = kThreads * ITEMS;
     __shared__ uint32_t s_k[TILE];
     __shared__ uint32_t s_next[256];  // histogram of the next pass's digit over this CTA's tiles
@@ -207,6 +208,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_pass0(BpScratch S, const uint32
                                                       const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
                                                       uint32_t* __restrict__ vout, const uint32_t* count_ptr,
                                                       uint32_t cap) {
+    pdl_wait();
     constexpr int TILE = kThreads * ITEMS;
     __shared__ uint32_t s_k[TILE];
     __shared__ uint32_t s_v[TILE];
@@ -284,7 +286,7 @@ cudaError_t launch_pass0(const BpScratch& s, const uint32_t* kin, const uint32_t
         return sm_count() * (per_sm > 0 ? per_sm : 1);
     });
     const uint32_t c = cap > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)cap;
-    k_pass0<kSortItems><<<grid, kThreads, 0, st>>>(s, kin, vin, kout, vout, count_ptr, c);
+    launch_pdl(k_pass0<kSortItems>, grid, kThreads, 0, st, s, kin, vin, kout, vout, count_ptr, c);
     return cudaGetLastError();
 }
 
@@ -298,6 +300,7 @@ cudaError_t launch_pass0(const BpScratch& s, const uint32_t* kin, const uint32_t
 constexpr int kGatherU = 4;
 __global__ void __launch_bounds__(kThreads) k_gather(BpScratch S, SortGather G, const uint32_t* __restrict__ vals,
                                                     const uint32_t* count_ptr, uint32_t cap) {
+    pdl_wait();
     const uint32_t n = min(*count_ptr, cap);
     const uint32_t stride = gridDim.x * kThreads;
     for (uint32_t g0 = blockIdx.x * kThreads + threadIdx.x; g0 < n; g0 += stride * kGatherU) {
@@ -341,7 +344,7 @@ cudaError_t launch_gather(const BpScratch& s, const SortGather& G, const uint32_
         return sm_count() * (per_sm > 0 ? per_sm : 1);
     });
     const uint32_t c = cap > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)cap;
-    k_gather<<<grid, kThreads, 0, st>>>(s, G, vals, count_ptr, c);
+    launch_pdl(k_gather, grid, kThreads, 0, st, s, G, vals, count_ptr, c);
     return cudaGetLastError();
 }
 
@@ -349,6 +352,7 @@ cudaError_t launch_gather(const BpScratch& s, const SortGather& G, const uint32_
 template <int PASSES>
 __global__ void __launch_bounds__(kThreads) k_hist(Ctrl* C, const uint32_t* __restrict__ keys, uint32_t n,
                                                    int flip) {
+    pdl_wait();
     __shared__ uint32_t s_hist[PASSES][256];
     for (uint32_t k = threadIdx.x; k < PASSES * 256; k += kThreads) (&s_hist[0][0])[k] = 0u;
     __syncthreads();
@@ -366,6 +370,7 @@ __global__ void __launch_bounds__(kThreads) k_hist(Ctrl* C, const uint32_t* __re
 
 // Counter reset + new epoch for a standalone sort.
 __global__ void k_sort_reset(Ctrl* C, uint32_t n, uint32_t* count_slot) {
+    pdl_wait();
     uint32_t t = threadIdx.x;
     for (uint32_t k = t; k < kHistWords; k += 256u) (&C->hist[0][0])[k] = 0u;
     if (t == 0) {
@@ -377,13 +382,13 @@ __global__ void k_sort_reset(Ctrl* C, uint32_t n, uint32_t* count_slot) {
 
 cudaError_t launch_sort_prep(const BpScratch& s, const uint32_t* keys, const uint32_t* count_ptr, uint32_t n,
                              int passes, cudaStream_t st, int flip) {
-    k_sort_reset<<<1, 256, 0, st>>>(s.ctrl, n, const_cast<uint32_t*>(count_ptr));
+    launch_pdl(k_sort_reset, 1, 256, 0, st, s.ctrl, n, const_cast<uint32_t*>(count_ptr));
     int grid = sm_count() * 4;
     switch (passes) {
-        case 1: k_hist<1><<<grid, kThreads, 0, st>>>(s.ctrl, keys, n, flip); break;
-        case 2: k_hist<2><<<grid, kThreads, 0, st>>>(s.ctrl, keys, n, flip); break;
-        case 3: k_hist<3><<<grid, kThreads, 0, st>>>(s.ctrl, keys, n, flip); break;
-        default: k_hist<4><<<grid, kThreads, 0, st>>>(s.ctrl, keys, n, flip); break;
+        case 1: launch_pdl(k_hist<1>, grid, kThreads, 0, st, s.ctrl, keys, n, flip); break;
+        case 2: launch_pdl(k_hist<2>, grid, kThreads, 0, st, s.ctrl, keys, n, flip); break;
+        case 3: launch_pdl(k_hist<3>, grid, kThreads, 0, st, s.ctrl, keys, n, flip); break;
+        default: launch_pdl(k_hist<4>, grid, kThreads, 0, st, s.ctrl, keys, n, flip); break;
     }
     return cudaGetLastError();
 }
@@ -407,11 +412,11 @@ cudaError_t launch_sort_pass(const BpScratch& s, int pass, int passes, const uin
     uint32_t c = cap > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)cap;
     const int next = (count_next && pass + 1 < passes) ? 1 : 0;
     if (small)
-        k_onesweep<kSortItemsSmall><<<grid, kThreads, 0, st>>>(s, kin, vin, kout, vout, count_ptr, c, pass, spin, G,
-                                                               next, fmode);
+        launch_pdl(k_onesweep<kSortItemsSmall>, grid, kThreads, 0, st, s, kin, vin, kout, vout, count_ptr, c, pass,
+                spin, G, next, fmode);
     else
-        k_onesweep<kSortItems><<<grid, kThreads, 0, st>>>(s, kin, vin, kout, vout, count_ptr, c, pass, spin, G, next,
-                                                          fmode);
+        launch_pdl(k_onesweep<kSortItems>, grid, kThreads, 0, st, s, kin, vin, kout, vout, count_ptr, c, pass, spin,
+                G, next, fmode);
     return cudaGetLastError();
 }
 

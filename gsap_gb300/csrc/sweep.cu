@@ -55,6 +55,7 @@ template <int MODE>
 __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const uint32_t* __restrict__ keys,
                                                     uint2* __restrict__ pairs,
                                                     uint64_t pair_cap, int count_rows) {
+    pdl_wait();
     __shared__ uint2 s_buf[kWarps][kBuf];
     // entries of the warp's chunk that have candidates, in run order
     // (boxes: (lo.xyz, jb), (hi.xyz, flags); spheres: (centre, radius),
@@ -267,8 +268,8 @@ cudaError_t launch_sweep(const BpScratch& s, const BpArgs& a, const uint32_t* ke
         else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep<1>, kThreads, 0);
         return sm_count() * (per_sm > 0 ? per_sm : 1);
     });
-    if (m == 0) k_sweep<0><<<grid, kThreads, 0, st>>>(s, a, keys, pairs, pair_cap, count_rows);
-    else k_sweep<1><<<grid, kThreads, 0, st>>>(s, a, keys, pairs, pair_cap, count_rows);
+    if (m == 0) launch_pdl(k_sweep<0>, grid, kThreads, 0, st, s, a, keys, pairs, pair_cap, count_rows);
+    else launch_pdl(k_sweep<1>, grid, kThreads, 0, st, s, a, keys, pairs, pair_cap, count_rows);
     return cudaGetLastError();
 }
 
