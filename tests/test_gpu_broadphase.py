@@ -521,6 +521,36 @@ def test_degenerate_and_far_from_origin_scenes(cuda, oracle_lib):
     assert np.array_equal(run_bp(sap, mn, mx, cuda), oracle_lib.bf_aabb(mn, mx))
 
 
+def test_rows_longer_than_the_shared_memory_sort(cuda, oracle_lib):
+    """Rows past the rank kernel's shared-memory sort (4096 pairs): two large
+    boxes (and spheres) each overlapping all 5,998 small ones, in the sorted
+    (i<j) form and the both-direction collision form."""
+    import torch
+    from gsap_gb300 import MODE_SPHERE, Sap
+    rng = np.random.default_rng(29)
+    n = 6000
+    c = rng.uniform(0, 30, (n, 3)).astype(np.float32)
+    h = rng.uniform(0.1, 0.4, (n, 3)).astype(np.float32)
+    c[:2] = 15.0
+    h[:2] = 20.0
+    mn = np.concatenate([c - h, np.zeros((n, 1), np.float32)], 1)
+    mx = np.concatenate([c + h, np.zeros((n, 1), np.float32)], 1)
+    got = run_bp(Sap(n), mn, mx, cuda)
+    assert np.count_nonzero(got[:, 0] == 0) == n - 1
+    assert np.array_equal(got, oracle_lib.bf_aabb(mn, mx))
+    r = np.full((n, 1), 0.3, np.float32)
+    r[:2] = 30.0
+    sp = np.concatenate([c, r], 1)
+    ssap = Sap(n, mode=MODE_SPHERE)
+    pairs = torch.empty((16 * n, 2), dtype=torch.int32, device=cuda)
+    ent = torch.empty(n + 1, dtype=torch.int32, device=cuda)
+    n_pairs, n_ent = ssap.collision(0.0, torch.from_numpy(sp).to(cuda), pairs, ent)
+    want_pairs, want_ent = oracle_lib.both_directions(oracle_lib.bf_sphere(sp))
+    assert n_pairs == len(want_pairs) and n_ent == len(want_ent)
+    assert np.array_equal(pairs[:n_pairs].cpu().numpy(), want_pairs)
+    assert np.array_equal(ent[:n_ent].cpu().numpy(), want_ent)
+
+
 @pytest.mark.parametrize("both", [False, True])
 def test_sparse_pairs_reset_row_counters_between_calls(cuda, oracle_lib, both):
     """Few pairs against many objects (fewer than n / 4): the scatter, not
