@@ -469,6 +469,16 @@ def run_ours(args, world, rank, local):
     return line
 
 
+def fixed_settings(args):
+    """Sap settings from the command line (--no-tune): key width, cell
+    factor, sort and radix tile, with the untuned defaults."""
+    kw = dict(sort_bits=args.sort_bits or 32, cell_factor=args.cell_factor or 2.0,
+              sort_mode={"radix": 0, "bucket": 1}[args.sort or "radix"], sort_tile=args.sort_tile or 4096)
+    desc = {"sort_bits": kw["sort_bits"], "cell_factor": kw["cell_factor"], "sort": args.sort or "radix",
+            "sort_tile": kw["sort_tile"], "autotuned": False}
+    return kw, desc
+
+
 def _extra_small(args, dev, stream, out):
     import torch
 
@@ -482,7 +492,8 @@ def _extra_small(args, dev, stream, out):
     # the reference's own CPU path for it is the O(n^2) brute force
     smn, smx = scenes.aabb_uniform(16384, 0)
     dsmn, dsmx = torch.from_numpy(smn).to(dev), torch.from_numpy(smx).to(dev)
-    ssap = Sap(16384)
+    skw, sdesc = fixed_settings(args)
+    ssap = Sap(16384, **skw) if args.no_tune else Sap(16384)
     spairs = torch.empty((16 * 16384, 2), dtype=torch.int32, device=dev)
     scnt = torch.zeros(1, dtype=torch.int64, device=dev)
     # autotuner (set-up, untimed), as for the 1M workload
@@ -500,7 +511,7 @@ def _extra_small(args, dev, stream, out):
     torch.cuda.synchronize()
     ssap.check()
     small = {"n": 16384, "pairs": int(scnt.item()), "ms_per_call": round(e0.elapsed_time(e1) / 200, 4),
-             "settings": dict(stuned, autotuned=True) if stuned else {"autotuned": False}}
+             "settings": dict(stuned, autotuned=True) if stuned else sdesc}
     if not args.no_cpu:
         import oracle
         oracle.build()
@@ -537,7 +548,8 @@ def _extra_demo(args, dev, stream, out):
     dprb = dd.system
     dsph = torch.from_numpy(dprb.get_particles()["p_pos"]).to(dev)
     nsp = dsph.shape[0]
-    csap = Sap(nsp, mode=1)
+    ckw, cdesc = fixed_settings(args)
+    csap = Sap(nsp, mode=1, **ckw) if args.no_tune else Sap(nsp, mode=1)
     cpairs = torch.empty((40 * nsp, 2), dtype=torch.int32, device=dev)
     cent = torch.empty(nsp + 1, dtype=torch.int32, device=dev)
     # autotuner (set-up, untimed) on the same spheres; the collision calls use its settings
@@ -555,7 +567,7 @@ def _extra_demo(args, dev, stream, out):
             "ms_per_call": round((time.perf_counter() - h0) * 10, 4),
             "device_ms_per_call": round(e0.elapsed_time(e1) / 100, 4),
             "note": "gsap_sap_collision blocks for the host counts each call, as Sap::collision does",
-            "settings": dict(ctuned, autotuned=True) if ctuned else {"autotuned": False}}
+            "settings": dict(ctuned, autotuned=True) if ctuned else cdesc}
     if not args.no_cpu:
         import oracle
         sp = dsph.cpu().numpy()
@@ -709,14 +721,16 @@ def _extra_rigid(args, dev, stream, out):
     prb.load_scene(sc)
     prb.set_contact(model=CONTACT_CONFIG, **cfgp)
     init = {k: np.ascontiguousarray(sc[k], np.float32) for k in ("pos", "quat", "lin_vel", "ang_vel")}
-    rsap = Sap(nb, sort_bits=24)
+    rkw, rdesc = fixed_settings(args)
+    rkw["sort_bits"] = rdesc["sort_bits"] = args.sort_bits or 24
+    rsap = Sap(nb, **rkw)
     # autotuner (set-up, untimed) on the body AABBs of the initial pose
     rtuned = None
     if not args.no_tune:
         bmn, bmx = scenes.body_aabbs(sc)
         rtuned = rsap.autotune(torch.from_numpy(bmn).to(dev), torch.from_numpy(bmx).to(dev), reps=20, stream=stream)
     rb = {"bodies": nb, "particles": sc["n_particles"],
-          "broadphase_settings": dict(rtuned, autotuned=True) if rtuned else {"autotuned": False, "sort_bits": 24}}
+          "broadphase_settings": dict(rtuned, autotuned=True) if rtuned else rdesc}
     if not args.no_cpu:
         import oracle
         from oracle.trajectory import fp64_errors

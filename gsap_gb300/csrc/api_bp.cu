@@ -354,13 +354,14 @@ static gsap_status record(gsap_sap* h, const Call& c, cudaStream_t st, bool time
         const bool separate = c.S > 1 && (uint64_t)c.n * 32ull > kGatherInPassBytes;
         for (int p = 0; p < passes; ++p) {
             const bool last = p == passes - 1 && !separate;
+            const uint64_t est = (uint64_t)c.n * kEstEntriesPerObject;
             if (p == 0)
                 CK(launch_pass0(s, s.keys[src], s.vals[src], s.keys[src ^ 1], s.vals[src ^ 1], count, s.entry_cap,
-                                st));
+                                st, est));
             else
                 CK(launch_sort_pass(s, p, passes, s.keys[src], s.vals[src], s.keys[src ^ 1],
                                     last ? nullptr : s.vals[src ^ 1], count, s.entry_cap, a.spin_limit, st,
-                                    last ? &gather : nullptr, true, 0, (int)h->cfg.sort_tile));
+                                    last ? &gather : nullptr, true, 0, (int)h->cfg.sort_tile, est));
             src ^= 1;
         }
         if (separate) CK(launch_gather(s, gather, s.vals[src], count, s.entry_cap, st));

@@ -466,11 +466,16 @@ cudaError_t launch_canonical(const BpScratch& s, uint32_t n, const uint2* in_pai
     if (scanned) launch_pdl(k_tilescan, 1, 1024, 0, st, s.tile_sums, ntiles);
     launch_pdl(k_rowscan, ntiles, kThreads, 0, st, s.rowcnt, s.rowoff, s.tile_sums, n, scanned, s.ctrl, in_cap);
     const uint64_t grp_cap = 2 * s.pair_cap_internal;
-    launch_pdl(k_scatter, sm_count() * 16, kThreads, 0, st, s, in_pairs, in_cap, s.grp_pairs, grp_cap, both, n);
-    launch_pdl(k_rank, sm_count() * 8, kThreads, 0, st, s, s.grp_pairs, grp_cap, n, out_pairs, out_cap);
-    launch_pdl(k_rowsort_long, sm_count() * 2, kThreads, 0, st, s, s.grp_pairs, out_pairs, out_cap);
-    if (both && entries) launch_pdl(k_scan<1>, grid, kThreads, 0, st, s, s.rowoff, nullptr, entries, entry_cap, n, 6,
-            spin);
+    const uint64_t est_pairs = (uint64_t)n * kEstPairsPerObject * (both ? 2u : 1u);
+    launch_pdl(k_scatter, call_grid(sm_count() * 16, est_pairs, kThreads * 4u), kThreads, 0, st, s, in_pairs, in_cap,
+            s.grp_pairs, grp_cap, both, n);
+    launch_pdl(k_rank, call_grid(sm_count() * 8, est_pairs, kRankTile), kThreads, 0, st, s, s.grp_pairs, grp_cap, n,
+            out_pairs, out_cap);
+    launch_pdl(k_rowsort_long, call_grid(sm_count() * 2, n, 4096u), kThreads, 0, st, s, s.grp_pairs, out_pairs,
+            out_cap);
+    if (both && entries)
+        launch_pdl(k_scan<1>, call_grid(grid, ntiles, 1u), kThreads, 0, st, s, s.rowoff, nullptr, entries, entry_cap,
+                n, 6, spin);
     return cudaGetLastError();
 }
 

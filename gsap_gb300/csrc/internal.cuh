@@ -225,12 +225,13 @@ struct SortGather {
 // them back as they are stored (last pass).
 enum : int { kSortFlipIn = 1, kSortUnflipOut = 2 };
 // tile: keys per tile, kSortTile or kSortTileMin (the status table must
-// hold 256 words per tile of that size).
+// hold 256 words per tile of that size).  keys_hint: an estimate of the key
+// count that sizes the grid (call_grid); 0 for the full-occupancy grid.
 cudaError_t launch_sort_pass(const BpScratch& s, int pass, int passes, const uint32_t* kin,
                              const uint32_t* vin, uint32_t* kout, uint32_t* vout,
                              const uint32_t* count_ptr, uint64_t cap, uint32_t spin, cudaStream_t st,
                              const SortGather* gather = nullptr, bool count_next = false, int fmode = 0,
-                             int tile = kSortTile);
+                             int tile = kSortTile, uint64_t keys_hint = 0);
 // Counter reset and the digit histograms of a standalone sort (flip != 0:
 // of the float images of the keys).
 cudaError_t launch_sort_prep(const BpScratch& s, const uint32_t* keys, const uint32_t* count_ptr,
@@ -244,7 +245,8 @@ cudaError_t launch_bucket_sort(const BpScratch& s, const SortGather& G, uint32_t
 // not order-preserving: entries of one digit may land in any order, which
 // the first pass of an LSD sort may do (the later passes are stable).
 cudaError_t launch_pass0(const BpScratch& s, const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
-                         uint32_t* vout, const uint32_t* count_ptr, uint64_t cap, cudaStream_t st);
+                         uint32_t* vout, const uint32_t* count_ptr, uint64_t cap, cudaStream_t st,
+                         uint64_t keys_hint = 0);
 // Sweep records of the sorted entries (put_record) from their sorted values
 // (object index | owner flags), after the last radix pass: a kernel of its
 // own at full occupancy, several entries' random bound loads in flight per
@@ -285,6 +287,22 @@ cudaError_t launch_canonical(const BpScratch& s, uint32_t n, const uint2* in_pai
                              uint2* out_pairs, uint64_t out_cap, int both, int32_t* entries,
                              uint64_t entry_cap, uint32_t spin, cudaStream_t st);
 int sm_count();
+
+// Grids of the persistent and grid-stride kernels (radix passes, sweep,
+// scatter, rank) are sized for the call: at most one CTA per `per` units of
+// an estimate of its work from the object count, and never more than the
+// full-occupancy grid.  Any grid covers all the work (tickets, work stealing
+// or grid-stride loops); the clamp spares a small call the hundreds of CTAs
+// that would find nothing to do, each of which still has to be scheduled
+// and run its prologue on the call's latency chain.
+inline int call_grid(int full, uint64_t work, uint64_t per) {
+    const uint64_t g = (work + per - 1) / per;
+    return (int)(g < 1 ? 1 : (g < (uint64_t)full ? g : (uint64_t)full));
+}
+// Estimates of a call's work from its object count n: sweep entries (cell
+// replication; about 2.3 per object at the 1M workload) and stored pairs.
+constexpr uint64_t kEstEntriesPerObject = 4;
+constexpr uint64_t kEstPairsPerObject = 8;
 
 // ------------------------------------------------------------ device helpers
 #ifdef __CUDACC__

@@ -277,14 +277,16 @@ __global__ void __launch_bounds__(kThreads, 2) k_pass0(BpScratch S, const uint32
 }
 
 cudaError_t launch_pass0(const BpScratch& s, const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
-                         uint32_t* vout, const uint32_t* count_ptr, uint64_t cap, cudaStream_t st) {
+                         uint32_t* vout, const uint32_t* count_ptr, uint64_t cap, cudaStream_t st,
+                         uint64_t keys_hint) {
     static std::once_flag once[kMaxDevices];
     static int val[kMaxDevices];
-    const int grid = per_device(once, val, [] {
+    const int full = per_device(once, val, [] {
         int per_sm = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pass0<kSortItems>, kThreads, 0);
         return sm_count() * (per_sm > 0 ? per_sm : 1);
     });
+    const int grid = keys_hint ? call_grid(full, keys_hint, kSortTile) : full;
     const uint32_t c = cap > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)cap;
     launch_pdl(k_pass0<kSortItems>, grid, kThreads, 0, st, s, kin, vin, kout, vout, count_ptr, c);
     return cudaGetLastError();
@@ -396,19 +398,20 @@ cudaError_t launch_sort_prep(const BpScratch& s, const uint32_t* keys, const uin
 cudaError_t launch_sort_pass(const BpScratch& s, int pass, int passes, const uint32_t* kin, const uint32_t* vin,
                              uint32_t* kout, uint32_t* vout, const uint32_t* count_ptr, uint64_t cap,
                              uint32_t spin, cudaStream_t st, const SortGather* gather, bool count_next, int fmode,
-                             int tile) {
+                             int tile, uint64_t keys_hint) {
     SortGather G;
     if (gather) G = *gather;
     else G = SortGather{nullptr, nullptr, nullptr, nullptr};
     static std::once_flag once[2][kMaxDevices];
     static int val[2][kMaxDevices];
     const int small = tile == kSortTileMin ? 1 : 0;
-    const int grid = per_device(once[small], val[small], [small] {
+    const int full = per_device(once[small], val[small], [small] {
         int per_sm = 0;
         if (small) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_onesweep<kSortItemsSmall>, kThreads, 0);
         else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_onesweep<kSortItems>, kThreads, 0);
         return sm_count() * (per_sm > 0 ? per_sm : 1);
     });
+    const int grid = keys_hint ? call_grid(full, keys_hint, small ? kSortTileMin : kSortTile) : full;
     uint32_t c = cap > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)cap;
     const int next = (count_next && pass + 1 < passes) ? 1 : 0;
     if (small)

@@ -262,12 +262,14 @@ cudaError_t launch_sweep(const BpScratch& s, const BpArgs& a, const uint32_t* ke
     static std::once_flag once[2][kMaxDevices];
     static int val[2][kMaxDevices];
     const int m = a.mode == 1 ? 1 : 0;
-    const int grid = per_device(once[m], val[m], [m] {
+    const int full = per_device(once[m], val[m], [m] {
         int per_sm = 0;
         if (m == 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep<0>, kThreads, 0);
         else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep<1>, kThreads, 0);
         return sm_count() * (per_sm > 0 ? per_sm : 1);
     });
+    // one CTA per 512 estimated entries (two 32-entry chunks per warp)
+    const int grid = call_grid(full, (uint64_t)a.n * kEstEntriesPerObject, 2u * kWarps * 32u);
     if (m == 0) launch_pdl(k_sweep<0>, grid, kThreads, 0, st, s, a, keys, pairs, pair_cap, count_rows);
     else launch_pdl(k_sweep<1>, grid, kThreads, 0, st, s, a, keys, pairs, pair_cap, count_rows);
     return cudaGetLastError();
