@@ -1001,7 +1001,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cell-factor", type=float, default=None,
                     help="sweep cell size / mean projected width (default: autotuned)")
-    ap.add_argument("--sort-bits", type=int, default=None, choices=[24, 32], help="radix key width (default: autotuned)")
+    ap.add_argument("--sort-bits", type=int, default=None, choices=[16, 24, 32], help="radix key width (default: autotuned)")
     ap.add_argument("--sort", default=None, choices=["bucket", "radix"],
                     help="how the sweep entries are sorted (default: autotuned)")
     ap.add_argument("--sort-tile", type=int, default=None, choices=[2048, 4096],

@@ -159,7 +159,10 @@ extern "C" gsap_sap* gsap_sap_create(uint32_t max_n, const gsap_config* cfg) {
     if (c.entry_factor == 0) c.entry_factor = 8;
     if (c.pair_factor == 0) c.pair_factor = 16;
     if (c.sort_bits == 0) c.sort_bits = 32;
-    if (c.sort_bits != 24 && c.sort_bits != 32) { fail(GSAP_ERR_INVALID, "sort_bits must be 24 or 32"); return nullptr; }
+    if (c.sort_bits != 16 && c.sort_bits != 24 && c.sort_bits != 32) {
+        fail(GSAP_ERR_INVALID, "sort_bits must be 16, 24 or 32");
+        return nullptr;
+    }
     if (c.cell_factor <= 0.f) c.cell_factor = 2.0f;
     if (c.spin_limit == 0) c.spin_limit = kDefaultSpin;
     if (c.sort_mode != GSAP_SORT_BUCKET && c.sort_mode != GSAP_SORT_RADIX) {
@@ -545,8 +548,9 @@ extern "C" gsap_status gsap_broadphase_aabb(gsap_sap* h, const float* d_min, con
 // (more, shorter tiles: a longer look-back chain but more CTAs per SM); the
 // digit width stays 8 bits (11-bit digits would multiply the look-back
 // words and the per-tile digit counters by 8).  The key width sets the radix
-// passes (24 bits: three 8-bit digits, 32 bits: four) and the q resolution
-// of the sweep; the cell factor sets the cell edge on u2/u3 and with it the
+// passes (16 bits: two 8-bit digits, 24 bits: three, 32 bits: four), and
+// with the cells it shares the key with, the q resolution of the sweep and
+// the most cells the grid may have; the cell factor sets the cell edge on u2/u3 and with it the
 // replication (entries to sort) against the candidate run length (tests).
 // Any setting gives the same pair set; only the time differs.
 extern "C" gsap_status gsap_sap_autotune(gsap_sap* h, const float* d_min, const float* d_max,
@@ -561,7 +565,7 @@ extern "C" gsap_status gsap_sap_autotune(gsap_sap* h, const float* d_min, const 
     const uint32_t sort_grid[3][2] = {{GSAP_SORT_RADIX, (uint32_t)kSortTile},
                                       {GSAP_SORT_RADIX, (uint32_t)kSortTileMin},
                                       {GSAP_SORT_BUCKET, (uint32_t)kSortTile}};
-    const uint32_t bits_grid[2] = {24, 32};
+    const uint32_t bits_grid[3] = {16, 24, 32};
     const float cf_grid[5] = {1.0f, 1.5f, 2.0f, 2.5f, 3.0f};
     const gsap_config saved = h->cfg;
     cudaStream_t st = (cudaStream_t)stream;
@@ -573,6 +577,10 @@ extern "C" gsap_status gsap_sap_autotune(gsap_sap* h, const float* d_min, const 
     for (const auto& sm : sort_grid)
         for (uint32_t bits : bits_grid)
             for (float cf : cf_grid) {
+                // 16-bit keys leave room for at most 1024 cells: tried on
+                // single scenes of up to 2^18 objects only (beyond, or shared
+                // by a batch's scenes, the cells are too few to be worth it)
+                if (bits == 16 && (S > 1 || n > (1u << 18))) continue;
                 h->cfg.sort_mode = sm[0];
                 h->cfg.sort_tile = sm[1];
                 h->cfg.sort_bits = bits;

@@ -196,7 +196,7 @@ struct BpArgs {
     uint32_t num_work;         // upper bound of work items launched
     int mode;                  // 0 AABB, 1 sphere
     int axis_mode;             // 0 PCA, 1 reference axis
-    uint32_t key_bits;         // 24 or 32
+    uint32_t key_bits;         // 16, 24 or 32
     float cell_factor;
     uint32_t spin_limit;
 };

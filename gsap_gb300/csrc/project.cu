@@ -203,12 +203,12 @@ cudaError_t launch_project(const BpScratch& s, const BpArgs& a, int passes, cuda
     if (a.num_work <= kProjSmallWork) {
         constexpr int kSplit = kChunk / (kThreads * kProjItemsSmall);
         if (passes == 0) launch_pdl(k_project<0, kProjItemsSmall>, a.num_work * kSplit, kThreads, 0, st, s, a);
-        else if (passes == 3) launch_pdl(k_project<3, kProjItemsSmall>, a.num_work * kSplit, kThreads, 0, st, s, a);
+        else if (passes <= 3) launch_pdl(k_project<3, kProjItemsSmall>, a.num_work * kSplit, kThreads, 0, st, s, a);
         else launch_pdl(k_project<4, kProjItemsSmall>, a.num_work * kSplit, kThreads, 0, st, s, a);
     } else {
         constexpr int kSplit = kChunk / (kThreads * kProjItemsLarge);
         if (passes == 0) launch_pdl(k_project<0, kProjItemsLarge>, a.num_work * kSplit, kThreads, 0, st, s, a);
-        else if (passes == 3) launch_pdl(k_project<3, kProjItemsLarge>, a.num_work * kSplit, kThreads, 0, st, s, a);
+        else if (passes <= 3) launch_pdl(k_project<3, kProjItemsLarge>, a.num_work * kSplit, kThreads, 0, st, s, a);
         else launch_pdl(k_project<4, kProjItemsLarge>, a.num_work * kSplit, kThreads, 0, st, s, a);
     }
     return cudaGetLastError();

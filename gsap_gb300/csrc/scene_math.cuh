@@ -182,7 +182,7 @@ __host__ __device__ inline void choose_scene(const SceneSums& z, const BpArgs& A
     float sd = sqrtf(r2 * r3 * target / (nf > 1.f ? nf : 1.f));
     if (s < sd) s = sd;
     if (!(s > 0.f) || !isfinite(s)) s = r2 > r3 ? r2 : r3;
-    const int qmin = A.key_bits >= 32 ? 12 : 8;
+    const int qmin = A.key_bits >= 32 ? 12 : (A.key_bits >= 24 ? 8 : 6);  // q bits kept for u1
     const float bmax = ldexpf(1.f, (int)A.key_bits - qmin);
     const float share = nf / (float)(n_total > 0 ? n_total : 1u);
     float bcap = floorf(bmax * share);

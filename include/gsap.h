@@ -79,7 +79,7 @@ typedef struct gsap_config {
     uint32_t max_scenes;    /* scenes per batched call (>= 1) */
     uint32_t entry_factor;  /* sweep-entry capacity = entry_factor * max_n (0 -> 8) */
     uint32_t pair_factor;   /* internal pair capacity = pair_factor * max_n (0 -> 16) */
-    uint32_t sort_bits;     /* radix key width, 24 or 32 (0 -> 32) */
+    uint32_t sort_bits;     /* radix key width, 16, 24 or 32 (0 -> 32) */
     float cell_factor;      /* cell size / mean projected width on the secondary axes (0 -> 2.0) */
     uint32_t spin_limit;    /* iteration cap of every device-side wait (0 -> default) */
     uint32_t sort_mode;     /* GSAP_SORT_* : how the sweep entries are sorted (0 -> radix) */

@@ -18,7 +18,7 @@ def test_create_rejects_bad_configs(gsap_lib):
     from gsap_gb300._lib import Config
     c = Config()
     gsap_lib.gsap_config_default(C.byref(c))
-    c.sort_bits = 16
+    c.sort_bits = 20
     assert not gsap_lib.gsap_sap_create(1000, C.byref(c))
     assert "sort_bits" in last_error(gsap_lib)
     gsap_lib.gsap_config_default(C.byref(c))

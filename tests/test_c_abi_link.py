@@ -20,7 +20,7 @@ int main(void) {
     gsap_config c;
     gsap_config_default(&c);
     if (c.sort_bits != 32 || c.max_scenes != 1) return 1;
-    c.sort_bits = 16;
+    c.sort_bits = 20;
     if (gsap_sap_create(1000, &c) != NULL) return 2;
     if (strstr(gsap_last_error(), "sort_bits") == NULL) return 3;
     uint64_t n = 0;

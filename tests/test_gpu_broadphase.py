@@ -277,7 +277,7 @@ def test_autotune_keeps_the_pair_set(cuda, oracle_lib):
     sap = Sap(n)
     dmn, dmx = to_dev(mn, cuda), to_dev(mx, cuda)
     cfg = sap.autotune(dmn, dmx, reps=2)
-    assert cfg["sort_bits"] in (24, 32) and cfg["cell_factor"] in (1.0, 1.5, 2.0, 2.5, 3.0)
+    assert cfg["sort_bits"] in (16, 24, 32) and cfg["cell_factor"] in (1.0, 1.5, 2.0, 2.5, 3.0)
     for graph in (False, True):
         got = sap.broadphase(dmn, dmx, sorted=True, graph=graph).cpu().numpy().astype(np.uint32)
         assert np.array_equal(got, want)
@@ -295,7 +295,7 @@ def test_autotune_keeps_the_pair_set(cuda, oracle_lib):
 
 
 @pytest.mark.parametrize("sort_mode,sort_tile", [(0, 4096), (0, 2048), (1, 4096)])
-@pytest.mark.parametrize("sort_bits", [24, 32])
+@pytest.mark.parametrize("sort_bits", [16, 24, 32])
 @pytest.mark.parametrize("cell_factor", [0.5, 1.0, 2.0, 4.0])
 def test_every_setting_gives_the_same_pairs(cuda, oracle_lib, sort_bits, cell_factor, sort_mode, sort_tile):
     """Sort (bucket, or radix with 4096- or 2048-key tiles), key width and
