@@ -236,45 +236,51 @@ __global__ void __launch_bounds__(kThreads) k_pca_finish(BpScratch S, BpArgs A, 
         if (one && !temporal) epoch0 = S.ctrl->epoch;
     }
     // Combine the scene's partials in float-float (two-sum) arithmetic on the
-    // FP32 pipes: thread t merges items t, t+256, ..., then warps and the CTA
-    // merge in a fixed order (deterministic); only the final hi + lo pairs go
-    // to FP64 (GB300's FP64 lane rate makes an FP64 reduction tree slow).
-    float ah[kPcaQ], al[kPcaQ], am[3] = {0.f, 0.f, 0.f};
+    // FP32 pipes, one quantity per thread: thread t (quantity q = t % kQn,
+    // group g = t / kQn) merges partials g, g + kG, ... of its quantity, then
+    // kQn threads merge the kG group results in order (deterministic); only
+    // the final hi + lo pairs go to FP64 (GB300's FP64 lane rate makes an FP64
+    // reduction slow).  Every chain is at most nw / kG + kG merges long.
+    constexpr uint32_t kQn = kPcaQ + 3;  // the sums, then the three maxima
+    constexpr uint32_t kG = kThreads / kQn;
+    __shared__ float s_gh[kG][kQn], s_gl[kG][kQn];
+    __shared__ double s_tot[kQn];
+    {
+        const uint32_t q = tid % kQn, g = tid / kQn;
+        if (g < kG) {
+            const PcaPartial* P = S.partials + wfirst * split;
+            const float* ph = q < (uint32_t)kPcaQ ? &P->hi[q] : &P->hmax[q - kPcaQ];
+            const float* pl = q < (uint32_t)kPcaQ ? &P->lo[q] : &P->hmax[q - kPcaQ];
+            constexpr uint32_t kStride = sizeof(PcaPartial) / sizeof(float);
+            float h = 0.f, l = 0.f;
+            // kU partials' loads in flight at once, then their merges in order
+            constexpr int kU = 8;
+            for (uint32_t k0 = g; k0 < nw; k0 += kU * kG) {
+                float vh[kU], vl[kU];
 #pragma unroll
-    for (int q = 0; q < kPcaQ; ++q) { ah[q] = 0.f; al[q] = 0.f; }
-    for (uint32_t k = tid; k < nw; k += kThreads) {
-        const PcaPartial* P = &S.partials[wfirst * split + k];
+                for (int u = 0; u < kU; ++u) {
+                    const uint32_t k = k0 + u * kG;
+                    vh[u] = k < nw ? ph[(size_t)k * kStride] : 0.f;
+                    vl[u] = k < nw ? pl[(size_t)k * kStride] : 0.f;
+                }
 #pragma unroll
-        for (int q = 0; q < kPcaQ; ++q) kahan_merge(ah[q], al[q], P->hi[q], P->lo[q]);
-#pragma unroll
-        for (int q = 0; q < 3; ++q) am[q] = fmaxf(am[q], P->hmax[q]);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-        for (int q = 0; q < kPcaQ; ++q) {
-            float h2 = __shfl_down_sync(0xffffffffu, ah[q], o);
-            float l2 = __shfl_down_sync(0xffffffffu, al[q], o);
-            kahan_merge(ah[q], al[q], h2, l2);
+                for (int u = 0; u < kU; ++u) {
+                    if (q < (uint32_t)kPcaQ) kahan_merge(h, l, vh[u], vl[u]);
+                    else h = fmaxf(h, vh[u]);
+                }
+            }
+            s_gh[g][q] = h;
+            s_gl[g][q] = l;
         }
-#pragma unroll
-        for (int q = 0; q < 3; ++q) am[q] = fmaxf(am[q], __shfl_down_sync(0xffffffffu, am[q], o));
-    }
-    __shared__ float s_ff[kThreads / 32][2 * kPcaQ + 3];
-    __shared__ double s_tot[kPcaQ + 3];
-    if (lane == 0) {
-        for (int q = 0; q < kPcaQ; ++q) { s_ff[wid][q] = ah[q]; s_ff[wid][kPcaQ + q] = al[q]; }
-        for (int q = 0; q < 3; ++q) s_ff[wid][2 * kPcaQ + q] = am[q];
     }
     __syncthreads();
-    if (tid < kPcaQ) {
-        float h = s_ff[0][tid], l = s_ff[0][kPcaQ + tid];
-        for (int w = 1; w < kThreads / 32; ++w) kahan_merge(h, l, s_ff[w][tid], s_ff[w][kPcaQ + tid]);
-        s_tot[tid] = (double)h + (double)l;
-    } else if (tid < kPcaQ + 3) {
-        float m = s_ff[0][2 * kPcaQ + tid - kPcaQ];
-        for (int w = 1; w < kThreads / 32; ++w) m = fmaxf(m, s_ff[w][2 * kPcaQ + tid - kPcaQ]);
-        s_tot[tid] = (double)m;
+    if (tid < kQn) {
+        float h = s_gh[0][tid], l = s_gl[0][tid];
+        for (uint32_t g = 1; g < kG; ++g) {
+            if (tid < (uint32_t)kPcaQ) kahan_merge(h, l, s_gh[g][tid], s_gl[g][tid]);
+            else h = fmaxf(h, s_gh[g][tid]);
+        }
+        s_tot[tid] = tid < (uint32_t)kPcaQ ? (double)h + (double)l : (double)h;
     }
     __syncthreads();
     Ctrl* C = S.ctrl;

@@ -96,7 +96,7 @@ __host__ __device__ inline void choose_scene(const SceneSums& z, const BpArgs& A
     double C[3][3];
     const int idx[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
     for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) C[i][j] = z.sdd[idx[i][j]] * inv_n - md[i] * md[j];
+        for (int j = i; j < 3; ++j) C[i][j] = C[j][i] = z.sdd[idx[i][j]] * inv_n - md[i] * md[j];
     double mean[3] = {z.pilot[0] + md[0], z.pilot[1] + md[1], z.pilot[2] + md[2]};
 
     // From here on FP32 (the FP64 fields of the record are written from it):
@@ -117,7 +117,7 @@ __host__ __device__ inline void choose_scene(const SceneSums& z, const BpArgs& A
     } else {
         float a[3][3], v[3][3];
         for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j) a[i][j] = (float)(0.5 * (C[i][j] + C[j][i]));
+            for (int j = 0; j < 3; ++j) a[i][j] = (float)C[i][j];  // C is symmetric as built
         eig3(a, v);
         int o[3] = {0, 1, 2};
         float ev[3] = {a[0][0], a[1][1], a[2][2]};

@@ -227,6 +227,32 @@ def test_gauss_1m_against_cpu_sap(cuda, oracle_lib, axis_mode):
         assert abs(abs(ax @ R[:, 0]) - 1.0) < 1e-3
 
 
+@pytest.mark.parametrize("seed", range(3))
+def test_device_scene_solve_matches_numpy(cuda, seed):
+    """The scene solve as the GPU runs it (float-float sums of the box
+    centres, FP64 covariance, FP32 Jacobi) against numpy's FP64 eigh of the
+    same centres: eigenvalues within 2e-6 of the largest, axes orthonormal
+    to 1e-5 and aligned to ~2e-4 rad."""
+    from gsap_gb300 import Sap
+    rng = np.random.default_rng(seed)
+    R = np.linalg.qr(rng.normal(size=(3, 3)))[0]
+    n = 20000
+    pts = ((rng.normal(size=(n, 3)) * [40.0, 9.0, 2.0]) @ R.T + rng.normal(size=3) * 100).astype(np.float32)
+    h = np.float32(0.05)
+    mn = np.concatenate([pts - h, np.zeros((n, 1), np.float32)], 1)
+    mx = np.concatenate([pts + h, np.zeros((n, 1), np.float32)], 1)
+    sap = Sap(n)
+    run_bp(sap, mn, mx, cuda)
+    sc = sap.scene_axes()
+    U, eig = np.array(sc["axes"]), np.array(sc["eig"])
+    w, V = np.linalg.eigh(np.cov(pts.astype(np.float64).T, bias=True))
+    assert np.allclose(eig, w[::-1], rtol=0, atol=2e-6 * w.max())
+    assert np.allclose(U @ U.T, np.eye(3), atol=1e-5)
+    for k in range(3):
+        assert 1.0 - abs(U[k] @ V[:, 2 - k]) / np.linalg.norm(U[k]) < 2e-8
+    assert np.linalg.det(U) > 0
+
+
 def test_large_scene_sampled_rows_against_brute_force(cuda):
     """16,777,216 boxes (the 1M workload's object density at 16 times the
     objects; about 95M pairs): every reported pair overlaps, the list is
