@@ -577,6 +577,30 @@ def test_rows_longer_than_the_shared_memory_sort(cuda, oracle_lib):
     assert np.array_equal(ent[:n_ent].cpu().numpy(), want_ent)
 
 
+def test_chains_alternating_with_a_dense_scene(cuda, oracle_lib):
+    """Chains of boxes that each overlap only the next one (2047, 2048 and
+    2049 pairs, rows of one pair, shuffled ids, a rank-1 spread) alternating
+    on one handle with a dense scene: every call equals the brute force (a
+    row counter left behind by one call would shift the next call's rows)."""
+    from gsap_gb300 import Sap
+    rng = np.random.default_rng(37)
+    sap = Sap(8192)
+    dense_c = rng.uniform(0, 12, (6000, 3)).astype(np.float32)
+    dense_h = rng.uniform(0.2, 0.5, (6000, 3)).astype(np.float32)
+    dense = (np.concatenate([dense_c - dense_h, np.zeros((6000, 1), np.float32)], 1),
+             np.concatenate([dense_c + dense_h, np.zeros((6000, 1), np.float32)], 1))
+    for m in (2048, 2049, 2050, 2049):
+        x = np.arange(m, dtype=np.float32)
+        c = np.stack([x, np.zeros(m, np.float32), np.zeros(m, np.float32)], 1)[rng.permutation(m)]
+        h = np.float32([0.6, 0.5, 0.5])  # neighbours 1.0 apart overlap, next-but-one do not
+        mn = np.concatenate([c - h, np.zeros((m, 1), np.float32)], 1)
+        mx = np.concatenate([c + h, np.zeros((m, 1), np.float32)], 1)
+        want = oracle_lib.bf_aabb(mn, mx)
+        assert len(want) == m - 1
+        assert np.array_equal(run_bp(sap, mn, mx, cuda), want)
+        assert np.array_equal(run_bp(sap, *dense, cuda), oracle_lib.bf_aabb(*dense))
+
+
 @pytest.mark.parametrize("both", [False, True])
 def test_sparse_pairs_reset_row_counters_between_calls(cuda, oracle_lib, both):
     """Few pairs against many objects (fewer than n / 4): the scatter, not
