@@ -119,11 +119,19 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
     // With fewer entries than kGrab chunks for every warp of the grid (small
     // calls), one chunk at a time, so that the work spreads over all warps.
     const uint32_t grab = (uint64_t)E >= (uint64_t)gridDim.x * kWarps * 32u * kGrab ? 32u * kGrab : 32u;
+    // Entries for at most one chunk per warp (small calls): the warp's chunk
+    // is its own index, with no round trip to the counter before or after.
+    const bool one_chunk = (uint64_t)E <= (uint64_t)gridDim.x * kWarps * 32u;
+    // first gallop step: runs are tens of entries in large calls, a few in
+    // the sparse small ones
+    const uint32_t step0 = one_chunk ? 2u : 16u;
     uint32_t base = 0, grab_end = 0;
     while (true) {
         if (base >= grab_end) {
             uint32_t g = 0;
-            if (lane == 0) g = atomicAdd(&C->sweep_ctr, grab);
+            if (lane == 0)
+                g = !one_chunk ? atomicAdd(&C->sweep_ctr, grab)
+                               : (grab_end == 0 ? (blockIdx.x * kWarps + wid) * 32u : 0xFFFFFFFFu);
             base = __shfl_sync(0xffffffffu, g, 0);
             grab_end = base + grab;
         }
@@ -158,7 +166,7 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
             // last index with key <= kb: gallop from e with a first step near
             // the typical run length (tens of entries), then bisect
             // (lo: key <= kb, hi: key > kb or E)
-            uint32_t lo = e, hi = E, step = 16;
+            uint32_t lo = e, hi = E, step = step0;
             while (true) {
                 if (step >= E - lo) break;
                 const uint32_t p = lo + step;
