@@ -110,28 +110,39 @@ __host__ __device__ inline void choose_scene(const SceneSums& z, const BpArgs& A
         else ax = C[0][0] >= C[2][2] ? 0 : 2;
         int a1 = ax == 0 ? 1 : 0, a2 = 3 - ax - a1;
         int order[3] = {ax, a1, a2};
+        const double dg[3] = {C[0][0], C[1][1], C[2][2]};  // (no data-dependent index into C)
         for (int r = 0; r < 3; ++r) {
             for (int c = 0; c < 3; ++c) U[r][c] = (c == order[r]) ? 1.f : 0.f;
-            lam[r] = (float)C[order[r]][order[r]];
+            lam[r] = (float)(order[r] == 0 ? dg[0] : order[r] == 1 ? dg[1] : dg[2]);
         }
     } else {
         float a[3][3], v[3][3];
         for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 3; ++j) a[i][j] = (float)C[i][j];  // C is symmetric as built
         eig3(a, v);
-        int o[3] = {0, 1, 2};
+        // Descending eigenvalues, stable on ties (the compare-exchanges of a
+        // three-element bubble sort).  Columns are swapped with constant
+        // indices only, so that a, v and U stay in registers on the GPU (an
+        // index that depends on the data would put them in local memory,
+        // under every Jacobi update).
         float ev[3] = {a[0][0], a[1][1], a[2][2]};
-        // descending eigenvalues, stable on ties
-        for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 2 - i; ++j)
-                if (ev[o[j]] < ev[o[j + 1]]) { int t = o[j]; o[j] = o[j + 1]; o[j + 1] = t; }
+        auto order = [&](int i, int j) {
+            if (ev[i] < ev[j]) {
+                const float t = ev[i]; ev[i] = ev[j]; ev[j] = t;
+                for (int c = 0; c < 3; ++c) { const float w = v[c][i]; v[c][i] = v[c][j]; v[c][j] = w; }
+            }
+        };
+        order(0, 1);
+        order(1, 2);
+        order(0, 1);
         for (int r = 0; r < 3; ++r) {
-            lam[r] = ev[o[r]];
-            for (int c = 0; c < 3; ++c) U[r][c] = v[c][o[r]];
+            lam[r] = ev[r];
+            for (int c = 0; c < 3; ++c) U[r][c] = v[c][r];
             // sign: largest-magnitude component positive (lowest index on ties)
-            int m = 0;
-            for (int c = 1; c < 3; ++c) if (fabsf(U[r][c]) > fabsf(U[r][m])) m = c;
-            if (U[r][m] < 0.f) for (int c = 0; c < 3; ++c) U[r][c] = -U[r][c];
+            float big = U[r][0], abig = fabsf(U[r][0]);
+            if (fabsf(U[r][1]) > abig) { big = U[r][1]; abig = fabsf(U[r][1]); }
+            if (fabsf(U[r][2]) > abig) big = U[r][2];
+            if (big < 0.f) for (int c = 0; c < 3; ++c) U[r][c] = -U[r][c];
         }
         // right-handed frame
         U[2][0] = U[0][1] * U[1][2] - U[0][2] * U[1][1];
