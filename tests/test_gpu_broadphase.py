@@ -128,12 +128,16 @@ def test_nonfinite_input_is_reported(sap, cuda):
     assert len(run_bp(sap, mn, mx, cuda)) == 100 * 99 // 2
 
 
-def test_batched_matches_per_scene(cuda, oracle_lib):
+@pytest.mark.parametrize("sort_bits", [16, 32])
+def test_batched_matches_per_scene(cuda, oracle_lib, sort_bits):
+    """64 scenes in one batched call equal the per-scene brute force; with
+    16-bit keys the scenes share at most 1024 cells (one each here), so every
+    scene is swept along u1 alone."""
     import torch
     from gsap_gb300 import Sap, scenes
     mn, mx, off = scenes.batched_aabb(S=64, seed=3, lo=16, hi=3000)
     n = len(mn)
-    bsap = Sap(n, max_scenes=64)
+    bsap = Sap(n, max_scenes=64, sort_bits=sort_bits, pair_factor=64)
     got = bsap.broadphase_batched(to_dev(mn, cuda), to_dev(mx, cuda),
                                   torch.from_numpy(off.astype(np.int32)).to(cuda)).cpu().numpy().astype(np.uint32)
     want = []
