@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(kThreads) k_sweep(BpScratch S, BpArgs A, const
             uint32_t qh = (uint32_t)fminf(fmaxf(t, 0.f), qmax);
             const uint32_t kb = (key & ~qmask) | qh;  // >= key: q(hi1) >= q(lo1)
             // last index with key <= kb: gallop from e with a first step near
-            // the typical run length (tens of entries), then bisect
+            // the typical run length (step0), then bisect
             // (lo: key <= kb, hi: key > kb or E)
             uint32_t lo = e, hi = E, step = step0;
             while (true) {
