@@ -90,8 +90,7 @@ __device__ __forceinline__ void pilot_of(const BpArgs& A, uint32_t sb, uint32_t 
 // item.
 __global__ void __launch_bounds__(kThreads) k_pca(BpScratch S, BpArgs A, uint32_t split) {
     pdl_wait();
-    __shared__ float s_red[kThreads / 32][2 * kPcaQ + 3];
-    const uint32_t tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const uint32_t tid = threadIdx.x;
     uint32_t scene, b, e, wfirst, nw;
     if (!map_work(blockIdx.x / split, S, A, scene, b, e, wfirst, nw)) return;
     const uint32_t sb = scene_begin(A, scene), se = scene_end(A, scene);
@@ -107,12 +106,12 @@ __global__ void __launch_bounds__(kThreads) k_pca(BpScratch S, BpArgs A, uint32_
     // Each thread sums its (at most kChunk / kThreads = 16) objects in plain
     // FP32: d is taken about the pilot, so its terms are of the scene's
     // spread and 16 of them lose at most ~16 ulps.  From there on the sums
-    // are compensated: the warp, CTA and cross-CTA merges carry (hi, lo)
-    // pairs.  (Compensating every object's terms cost ~120 FP32 operations
-    // per object and made the kernel issue-bound on large batches.)
-    float hi[kPcaQ], lo[kPcaQ], hm[3] = {0.f, 0.f, 0.f};
+    // are compensated: the CTA and cross-CTA merges carry (hi, lo) pairs.
+    // (Compensating every object's terms cost ~120 FP32 operations per
+    // object and made the kernel issue-bound on large batches.)
+    float hi[kPcaQ], hm[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-    for (int q = 0; q < kPcaQ; ++q) { hi[q] = 0.f; lo[q] = 0.f; }
+    for (int q = 0; q < kPcaQ; ++q) hi[q] = 0.f;
     bool bad = false;
     constexpr int U = 4;  // objects in flight per thread
     for (uint32_t i0 = b + tid; i0 < e; i0 += U * kThreads) {
@@ -152,33 +151,47 @@ __global__ void __launch_bounds__(kThreads) k_pca(BpScratch S, BpArgs A, uint32_
         }
     }
     if (bad) atomicOr(&S.ctrl->error, kErrNonFinite);
-    // warp, then CTA, compensated reduction
+    // CTA reduction, one quantity per thread: every thread's sums go to
+    // shared memory (rows of kQn words: an odd stride, no bank conflicts),
+    // thread (q = t % kQn, g = t / kQn) merges rows g, g + kG, ... of
+    // column q as compensated pairs, and kQn threads merge the kG group
+    // results in order (deterministic).  Every chain is at most
+    // kThreads / kG + kG merges long, against five shuffle levels of all 21
+    // quantities in every warp.
+    constexpr uint32_t kQn = kPcaQ + 3;
+    constexpr uint32_t kG = kThreads / kQn;
+    __shared__ float s_v[kThreads][kQn];
+    __shared__ float s_gh[kG][kQn], s_gl[kG][kQn];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
+    for (int q = 0; q < kPcaQ; ++q) s_v[tid][q] = hi[q];
 #pragma unroll
-        for (int q = 0; q < kPcaQ; ++q) {
-            float h2 = __shfl_down_sync(0xffffffffu, hi[q], o);
-            float l2 = __shfl_down_sync(0xffffffffu, lo[q], o);
-            kahan_merge(hi[q], lo[q], h2, l2);
+    for (int k = 0; k < 3; ++k) s_v[tid][kPcaQ + k] = hm[k];
+    __syncthreads();
+    {
+        const uint32_t q = tid % kQn, g = tid / kQn;
+        if (g < kG) {
+            float h = 0.f, l = 0.f;
+            for (uint32_t r = g; r < (uint32_t)kThreads; r += kG) {
+                if (q < (uint32_t)kPcaQ) kahan_merge(h, l, s_v[r][q], 0.f);
+                else h = fmaxf(h, s_v[r][q]);
+            }
+            s_gh[g][q] = h;
+            s_gl[g][q] = l;
         }
-#pragma unroll
-        for (int k = 0; k < 3; ++k) hm[k] = fmaxf(hm[k], __shfl_down_sync(0xffffffffu, hm[k], o));
-    }
-    if (lane == 0) {
-        for (int q = 0; q < kPcaQ; ++q) { s_red[wid][q] = hi[q]; s_red[wid][kPcaQ + q] = lo[q]; }
-        for (int k = 0; k < 3; ++k) s_red[wid][2 * kPcaQ + k] = hm[k];
     }
     __syncthreads();
-    if (tid < kPcaQ) {
-        float h = s_red[0][tid], l = s_red[0][kPcaQ + tid];
-        for (int w = 1; w < kThreads / 32; ++w) kahan_merge(h, l, s_red[w][tid], s_red[w][kPcaQ + tid]);
-        S.partials[blockIdx.x].hi[tid] = h;
-        S.partials[blockIdx.x].lo[tid] = l;
-    } else if (tid < kPcaQ + 3) {
-        int k = tid - kPcaQ;
-        float m = s_red[0][2 * kPcaQ + k];
-        for (int w = 1; w < kThreads / 32; ++w) m = fmaxf(m, s_red[w][2 * kPcaQ + k]);
-        S.partials[blockIdx.x].hmax[k] = m;
+    if (tid < kQn) {
+        float h = s_gh[0][tid], l = s_gl[0][tid];
+        for (uint32_t g = 1; g < kG; ++g) {
+            if (tid < (uint32_t)kPcaQ) kahan_merge(h, l, s_gh[g][tid], s_gl[g][tid]);
+            else h = fmaxf(h, s_gh[g][tid]);
+        }
+        if (tid < (uint32_t)kPcaQ) {
+            S.partials[blockIdx.x].hi[tid] = h;
+            S.partials[blockIdx.x].lo[tid] = l;
+        } else {
+            S.partials[blockIdx.x].hmax[tid - kPcaQ] = h;
+        }
     }
 }
 
