@@ -128,6 +128,18 @@ def test_grid_respects_entry_bound(gsap_lib):
         assert worst <= 8 * len(pts) + 4096
 
 
+@pytest.mark.parametrize("key_bits,qmin", [(16, 6), (24, 8), (32, 12)])
+def test_grid_leaves_the_key_its_q_bits(gsap_lib, key_bits, qmin):
+    """Whatever the object count, the cells of a one-scene grid take at most
+    key_bits - qmin bits of the sweep key (16-bit keys: at most 1024 cells),
+    so the quantised lower bound keeps at least qmin bits."""
+    rng = np.random.default_rng(3)
+    for n in (500, 16384, 200000):
+        pts = rng.uniform(0, 100, (n, 3))
+        U, eig, mean, G2, G3 = solve(gsap_lib, pts, np.full((n, 3), 0.05), key_bits=key_bits)
+        assert 1 <= G2 * G3 <= 2 ** (key_bits - qmin)
+
+
 def test_demo_scene_and_snapshot_round_trip(tmp_path):
     """The headless demo's scene (DemoParticles::init layout) and its binary
     snapshots; no GPU needed."""
